@@ -1,0 +1,132 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+The oracle is a plain C++ restatement of the reference's octree smoke step
+(oracle/smoke_oracle.cpp).  Only the tests, the smoke check and the CPU-baseline leg of
+bench.py use it, as the checker; the CUDA library never loads it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRC = os.path.join(HERE, "smoke_oracle.cpp")
+SCENE = os.path.join(ROOT, "ast-grid_gb300", "csrc")
+
+# array names and element types exposed by orc_get
+F64 = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
+       "tilt_e", "w_mac", "w_tilt", "A_val", "b", "p", "pcg_err", "ambT", "dual_tables"}
+I32 = {"tilt_flags", "slot_coords", "level_sizes", "split_map", "pindex_oct", "pindex_tilt", "A_rowptr",
+       "A_col", "pcg_iters", "anomalies"}
+I64 = {"half_tilts", "t_joints", "closed_by_half_tilt"}
+U8 = {"tilt_open"}
+SHAPES = {"mac": (3, -1), "tilt_vel": (-1, 8), "dual_oct": (-1, 3), "dual_tilt": (-1, 3), "tilt_flags": (-1, 2),
+          "slot_coords": (-1, 4), "level_sizes": (-1, 3), "w_mac": (3, -1), "w_tilt": (-1, 8),
+          "dual_tables": (128, 3, 7)}
+
+
+def build(force=False):
+    """Compile the oracle with g++ (IEEE order: no fast-math, no FP contraction)."""
+    os.makedirs(BUILD, exist_ok=True)
+    deps = [SRC, os.path.join(SCENE, "scene.h")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
+        return LIB
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", SCENE, SRC, "-o", LIB + ".tmp"]
+    subprocess.check_call(cmd)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("buoy_d", ctypes.c_double), ("buoy_t", ctypes.c_double),
+                ("decay", ctypes.c_double), ("rho", ctypes.c_double), ("noise", ctypes.c_double),
+                ("src_cx", ctypes.c_double), ("src_cy", ctypes.c_double), ("src_cz", ctypes.c_double),
+                ("src_r", ctypes.c_double), ("seed", ctypes.c_ulonglong), ("max_iter", ctypes.c_int),
+                ("tilt_adaptivity", ctypes.c_int), ("closed_mask", ctypes.c_int), ("reduce_mode", ctypes.c_int),
+                ("ref_workers", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        _lib.orc_create.restype = ctypes.c_void_p
+        _lib.orc_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(_Params), ctypes.c_char_p, ctypes.c_int]
+        _lib.orc_destroy.argtypes = [ctypes.c_void_p]
+        _lib.orc_stage.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_char_p, ctypes.c_int]
+        _lib.orc_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_char_p, ctypes.c_int]
+        _lib.orc_get.restype = ctypes.c_longlong
+        _lib.orc_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_longlong]
+        _lib.orc_set.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_longlong]
+        _lib.orc_size.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    return _lib
+
+
+class Oracle:
+    """One oracle solver on the benchmark scene (z-up, sphere source, closed walls but the top)."""
+
+    def __init__(self, coarsest, levels, tol=1e-6, buoy_d=-0.1, buoy_t=1.0, decay=1.0, rho=2.0, noise=1e-3,
+                 source=(0.5, 0.5, 0.12, 0.06), seed=0, max_iter=3000, tilt_adaptivity=True, closed_mask=47,
+                 reduce_mode=0, ref_workers=8):
+        """reduce_mode 0 follows the reference's own reduction order (Eigen's dot, per-worker
+        partial sums over ref_workers workers); 1 follows the CUDA library's fixed tree."""
+        p = _Params(tol, buoy_d, buoy_t, decay, rho, noise, source[0], source[1], source[2], source[3], seed,
+                    max_iter, 1 if tilt_adaptivity else 0, closed_mask, reduce_mode, ref_workers)
+        err = ctypes.create_string_buffer(512)
+        self._h = lib().orc_create(coarsest, levels, ctypes.byref(p), err, 512)
+        if not self._h:
+            raise RuntimeError("oracle: " + err.value.decode())
+
+    def close(self):
+        if self._h:
+            lib().orc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc, err):
+        if rc != 0:
+            raise RuntimeError("oracle: " + err.value.decode())
+
+    def stage(self, i, dt):
+        err = ctypes.create_string_buffer(512)
+        self._check(lib().orc_stage(self._h, i, dt, err, 512), err)
+
+    def step(self, dt):
+        err = ctypes.create_string_buffer(512)
+        self._check(lib().orc_step(self._h, dt, err, 512), err)
+
+    def get(self, name):
+        n = lib().orc_get(self._h, name.encode(), None, 0)
+        if n < 0:
+            raise KeyError(name)
+        dt = np.float64 if name in F64 else np.int32 if name in I32 else np.int64 if name in I64 else np.uint8
+        out = np.empty(n, dtype=dt)
+        lib().orc_get(self._h, name.encode(), out.ctypes.data, n)
+        if name in SHAPES:
+            out = out.reshape(SHAPES[name])
+        return out
+
+    def set(self, name, arr):
+        base = name[2:] if name.startswith("t_") else name
+        dt = np.int32 if base == "tilt_flags" else np.uint8 if base == "tilt_open" else np.float64
+        a = np.ascontiguousarray(arr, dtype=dt).ravel()
+        rc = lib().orc_set(self._h, name.encode(), a.ctypes.data, a.size)
+        if rc != 0:
+            raise ValueError(f"oracle: cannot set {name} ({rc})")
+
+    @property
+    def slots(self):
+        return lib().orc_size(self._h, 0)
+
+    @property
+    def ndof(self):
+        return lib().orc_size(self._h, 3)

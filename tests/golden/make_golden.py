@@ -1,0 +1,66 @@
+"""Regenerate the golden fixtures from the reference solver itself.
+
+Builds the reference's own sources with oracle/ref/Makefile (reference checkout at $ASTG_REF,
+default /root/reference), runs the fixture harness oracle/ref/ref_harness.cpp on small cases
+of the benchmark scene, and stores the dumps as compressed .npz files next to this script.
+
+    python tests/golden/make_golden.py
+
+Fixture keys (all arrays in the reference's slot order, see oracle/smoke_oracle.cpp):
+  layout: level_sizes, slot_coords, split_map, half_tilts, t_joints, closed_by_half_tilt,
+          w_mac, w_tilt, dual_tables, init/<field>, init/t_<field>
+  per step k (1-based) final state: step<k>/<field>, step<k>/t_<field>, and the projection of
+          that step: step<k>/A_rowptr, A_col, A_val, b, p, pcg_iters, pindex_oct, pindex_tilt, ambT
+  stage snapshots of step 1 (when recorded): stage1_<name>/<field>, t_<field>
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+import astg_archive  # noqa: E402
+
+CASES = [
+    # name, coarsest, levels, steps, record stage snapshots of step 1
+    ("ref_c8_l3", 8, 3, 4, True),
+    ("ref_c16_l2", 16, 2, 3, False),
+]
+STAGES = ["scene", "force", "preproject", "project", "dual", "advect"]
+
+
+def main():
+    ref = os.environ.get("ASTG_REF", "/root/reference")
+    subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref", "Makefile"), f"REF={ref}",
+                           "-j8"])
+    harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+    for name, c, lv, steps, stages in CASES:
+        with tempfile.TemporaryDirectory() as d:
+            cmd = [harness, "--coarsest", str(c), "--levels", str(lv), "--steps", str(steps), "--out", d]
+            if stages:
+                cmd.append("--stages")
+            subprocess.check_call(cmd)
+            out = {}
+            lay = astg_archive.read(os.path.join(d, "layout.astg"))
+            out.update(lay)
+            for k in range(1, steps + 1):
+                st = astg_archive.read(os.path.join(d, f"step_{k:04d}.astg"))
+                for key, v in st.items():
+                    if key != "wall_s":
+                        out[f"step{k}/{key}"] = v
+            if stages:
+                st = astg_archive.read(os.path.join(d, "stages_0001.astg"))
+                for key, v in st.items():
+                    out[key.replace("s0_", "stage1_", 1)] = v
+            out["meta/case"] = np.array([c, lv, steps], dtype=np.int32)
+            path = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(path, **out)
+            print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB, {len(out)} arrays")
+
+
+if __name__ == "__main__":
+    main()
