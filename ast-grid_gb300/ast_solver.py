@@ -1,0 +1,220 @@
+"""Python front end of the GB300 octree smoke step (module name and entry points follow the
+reference's pybind module ``ast_solver``, python_bindings/ast_solver.cc:14-80).
+
+``OctreeSmoke3`` wraps OctreeOmniGridSolver3 (include/octree_omnigrid_solver3.h:23-57) through
+the C ABI of include/astg.h.  The library must be built (``build_lib.build()``); importing this
+module on a machine without it raises instead of falling back to anything.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libastgrid_gpu.so")
+
+ASTG_OK, ASTG_BAD_ARG, ASTG_CUDA_ERROR, ASTG_NOT_CONVERGED = 0, 1, 2, 3
+ASTG_DEVICE_WAIT_TIMEOUT, ASTG_NAN_DETECTED, ASTG_LAYOUT_ERROR, ASTG_NO_DEVICE = 4, 5, 6, 7
+STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "device wait timeout",
+          5: "NaN detected", 6: "layout error", 7: "no CUDA device"}
+FP64, MIXED = 0, 1
+
+# exported symbols of include/astg.h
+SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_stage",
+           "astg_set_solver_parameters", "astg_set_precision", "astg_last_solve", "astg_size", "astg_get", "astg_set",
+           "astg_solve", "astg_max_velocity"]
+
+
+class AstgError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("coarsest", ctypes.c_int), ("levels", ctypes.c_int), ("tol", ctypes.c_double),
+                ("max_iter", ctypes.c_int), ("omega", ctypes.c_double), ("min_diag", ctypes.c_double),
+                ("rho", ctypes.c_double), ("buoy_density", ctypes.c_double), ("buoy_temp", ctypes.c_double),
+                ("decay", ctypes.c_double), ("closed_mask", ctypes.c_int), ("tilt_adaptivity", ctypes.c_int),
+                ("src_x", ctypes.c_double), ("src_y", ctypes.c_double), ("src_z", ctypes.c_double),
+                ("src_r", ctypes.c_double), ("noise", ctypes.c_double), ("seed", ctypes.c_uint64),
+                ("precision", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("outer", ctypes.c_int), ("converged", ctypes.c_int),
+                ("n", ctypes.c_int), ("nnz", ctypes.c_longlong), ("residual", ctypes.c_double),
+                ("tolerance", ctypes.c_double), ("ms", ctypes.c_double)]
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [("solve", SolveStats), ("ms_total", ctypes.c_double), ("ms_force", ctypes.c_double),
+                ("ms_project", ctypes.c_double), ("ms_advect", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib(path=None):
+    """Loads libastgrid_gpu.so (raises OSError when it has not been built)."""
+    global _lib
+    if _lib is None:
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise OSError(f"{p} is missing: build it with ast-grid_gb300/build_lib.py (nvcc, sm_103a)")
+        L = ctypes.CDLL(p)
+        c_p = ctypes.c_void_p
+        L.astg_default_params.argtypes = [ctypes.POINTER(Params), ctypes.c_int, ctypes.c_int]
+        L.astg_create.argtypes = [ctypes.POINTER(Params), ctypes.c_void_p, ctypes.POINTER(c_p)]
+        L.astg_destroy.argtypes = [c_p]
+        L.astg_last_error.argtypes = [c_p]
+        L.astg_last_error.restype = ctypes.c_char_p
+        L.astg_step.argtypes = [c_p, ctypes.c_double, ctypes.POINTER(StepStats)]
+        L.astg_stage.argtypes = [c_p, ctypes.c_int, ctypes.c_double]
+        L.astg_set_solver_parameters.argtypes = [c_p, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.astg_set_precision.argtypes = [c_p, ctypes.c_int]
+        L.astg_last_solve.argtypes = [c_p, ctypes.POINTER(SolveStats)]
+        L.astg_size.argtypes = [c_p, ctypes.c_int]
+        L.astg_size.restype = ctypes.c_longlong
+        L.astg_get.argtypes = [c_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+        L.astg_set.argtypes = [c_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t]
+        L.astg_solve.argtypes = [c_p, ctypes.c_int, c_p, c_p, c_p, c_p, c_p, ctypes.c_double, ctypes.c_int,
+                                 ctypes.c_int, ctypes.POINTER(SolveStats)]
+        L.astg_max_velocity.argtypes = [c_p, ctypes.POINTER(ctypes.c_double)]
+        _lib = L
+    return _lib
+
+
+_F64 = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
+        "tilt_e", "w_mac", "w_tilt", "dual_tables", "A_val", "b", "p", "ambT"}
+_I64 = {"half_tilts", "t_joints", "closed_by_half_tilt"}
+_U8 = {"tilt_open"}
+_SHAPES = {"mac": (3, -1), "tilt_vel": (-1, 8), "dual_oct": (-1, 3), "dual_tilt": (-1, 3), "tilt_flags": (-1, 2),
+           "slot_coords": (-1, 4), "level_sizes": (-1, 3), "w_mac": (3, -1), "w_tilt": (-1, 8),
+           "dual_tables": (128, 3, 7)}
+
+
+_FIELDS = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
+           "tilt_e", "tilt_flags", "tilt_open"}
+
+
+def _base(name):
+    """Field name without the "t_" prefix that addresses the swap-partner buffer."""
+    return name[2:] if name.startswith("t_") and name[2:] in _FIELDS else name
+
+
+def _dtype(name):
+    base = _base(name)
+    if base in _F64:
+        return np.float64
+    if base in _I64:
+        return np.int64
+    if base in _U8:
+        return np.uint8
+    return np.int32
+
+
+class OctreeSmoke3:
+    """GPU OctreeOmniGridSolver3 on the benchmark scene (or on a caller-supplied split map).
+
+    OctreeSmoke3(coarsest, levels, **params) builds the octree and initialises the fields
+    (ctor + initialize(), src/octree_omnigrid_solver3.cpp:45-149); update(dt) is one fixed-time
+    step (Solver::update with useFixedTimeStep, src/solver.cpp:8-46)."""
+
+    def __init__(self, coarsest, levels, split_map=None, **kw):
+        L = lib()
+        p = Params()
+        L.astg_default_params(ctypes.byref(p), coarsest, levels)
+        for k, v in kw.items():
+            if k == "source":
+                p.src_x, p.src_y, p.src_z, p.src_r = v
+            elif k == "precision":
+                p.precision = {"fp64": FP64, "mixed": MIXED}.get(v, v)
+            else:
+                setattr(p, k, v)
+        self.params = p
+        h = ctypes.c_void_p()
+        sm = None
+        if split_map is not None:
+            sm = np.ascontiguousarray(split_map, dtype=np.int32)
+        st = L.astg_create(ctypes.byref(p), sm.ctypes.data if sm is not None else None, ctypes.byref(h))
+        self._h = h
+        if st != ASTG_OK:
+            msg = L.astg_last_error(h).decode() if h.value else ""
+            if h.value:
+                L.astg_destroy(h)
+            self._h = None
+            raise AstgError(st, msg)
+        self.last_step = StepStats()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().astg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, allow=()):
+        if st != ASTG_OK and st not in allow:
+            raise AstgError(st, lib().astg_last_error(self._h).decode())
+        return st
+
+    def update(self, dt):
+        return self._check(lib().astg_step(self._h, dt, ctypes.byref(self.last_step)), allow=(ASTG_NOT_CONVERGED,))
+
+    def stage(self, i, dt):
+        self._check(lib().astg_stage(self._h, i, dt))
+
+    def set_solver_parameters(self, tol, max_iter, omega=0.97, min_diag=0.25):
+        self._check(lib().astg_set_solver_parameters(self._h, tol, max_iter, omega, min_diag))
+
+    def set_precision(self, prec):
+        self._check(lib().astg_set_precision(self._h, {"fp64": FP64, "mixed": MIXED}.get(prec, prec)))
+
+    def last_solve(self):
+        s = SolveStats()
+        self._check(lib().astg_last_solve(self._h, ctypes.byref(s)))
+        return s
+
+    def size(self, what):
+        return lib().astg_size(self._h, what)
+
+    @property
+    def slots(self):
+        return self.size(0)
+
+    def get(self, name):
+        need = ctypes.c_size_t(0)
+        st = lib().astg_get(self._h, name.encode(), None, 0, ctypes.byref(need))
+        if st != ASTG_BAD_ARG:  # a size query answers BAD_ARG with the size filled in
+            self._check(st)
+        if st == ASTG_BAD_ARG and need.value == 0 and lib().astg_last_error(self._h):
+            err = lib().astg_last_error(self._h).decode()
+            if "unknown" in err:
+                raise AstgError(st, err)
+        dt = _dtype(name)
+        out = np.empty(need.value // np.dtype(dt).itemsize, dtype=dt)
+        if out.size:
+            self._check(lib().astg_get(self._h, name.encode(), out.ctypes.data, need.value, None))
+        base = _base(name)
+        return out.reshape(_SHAPES[base]) if base in _SHAPES else out
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=_dtype(name)).ravel()
+        self._check(lib().astg_set(self._h, name.encode(), a.ctypes.data, a.nbytes))
+
+    # reference-style getters (copies, reference storage order)
+    def getDensity(self):
+        return self.get("density_oct")
+
+    def getHeat(self):
+        return self.get("heat_oct")
+
+    def max_velocity(self):
+        v = ctypes.c_double()
+        self._check(lib().astg_max_velocity(self._h, ctypes.byref(v)))
+        return v.value

@@ -1,0 +1,1041 @@
+// Host side of the GB300 octree smoke step: builds the octree topology once (it is static in
+// the reference, src/octree_omnigrid_solver3.cpp:60-149), uploads it as flat device tables,
+// sequences the kernels of each step on one CUDA stream and implements the C ABI of
+// include/astg.h.  All per-step work runs on the GPU; the host only launches and, for the
+// PCG's stopping test and the status word, reads a few bytes back.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#define ASTG_HD
+#include "astg.h"
+#include "astg_launch.h"
+#include "scene.h"
+
+using namespace astg;
+
+namespace {
+
+const int OCT_NB_H[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+const int TILT_NB_OCT_H[8][3] = {{0, 0, 0},  {-1, 0, 0},  {-1, -1, 0},  {0, -1, 0},
+                                 {0, 0, -1}, {-1, 0, -1}, {-1, -1, -1}, {0, -1, -1}};
+const int HALF_SLOT_H[6][5] = {{0, 3, 4, 7, 1}, {0, 1, 4, 5, 2}, {0, 1, 2, 3, 5},
+                               {1, 2, 5, 6, 0}, {2, 3, 6, 7, 4}, {4, 5, 6, 7, 3}};
+const double HALF_DIR_POS_H[6][3] = {{1, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 1, 0}, {0, 0, 1}};
+const int TILT_UP_SIGN_H[8][3] = {{1, 1, 1},   {-1, 1, 1}, {-1, -1, 1}, {1, -1, 1},
+                                  {-1, -1, 1}, {1, -1, 1}, {1, 1, 1},   {-1, 1, 1}};
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// host copy of a tilt-E node (include/tilt_e_node.h:15-56)
+struct HTilt {
+    double e = 0;
+    uint32_t f = TF_CLOSED;
+    int dir = 0;
+    bool has(uint32_t b) const { return (f & b) != 0; }
+    void put(uint32_t b, bool v) { f = v ? (f | b) : (f & ~b); }
+    void setE(double ne, double maxE = -1) {
+        if (has(TF_FIXED)) return;
+        if (ne <= 0) { put(TF_CLOSED, true); put(TF_LARGEST, false); ne = 0; }
+        else if (maxE > 0 && ne >= maxE) { put(TF_CLOSED, false); put(TF_LARGEST, true); ne = maxE; }
+        else { put(TF_CLOSED, false); put(TF_LARGEST, false); }
+        e = ne;
+    }
+    uint32_t packed() const { return (f & 0xff) | ((uint32_t)(dir + 1) << 8); }
+};
+
+}  // namespace
+
+struct astg_handle {
+    astg_params P{};
+    std::string err;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evA = nullptr, evB = nullptr;
+
+    // ---------------------------------------------------------------- topology (host)
+    int L = 0, res = 0, S = 0, H = 0;
+    double dx = 0;
+    std::vector<int> lres, loff, lN, lG;
+    std::vector<double> ldh;
+    std::vector<std::vector<int>> brick;  // per level: global slot or -1
+    std::vector<int> sx, sy, sz, slev, sflag;
+    std::vector<int32_t> split;
+    std::vector<int> half, tj, cbh;
+    std::vector<HTilt> te[2];
+    std::vector<uint8_t> tOpen, tFixed;
+    std::vector<double> wMac, wTilt, M37;
+
+    // ---------------------------------------------------------------- device
+    Dev d{};
+    Fields F[2]{};
+    int cur = 0;
+    uint8_t* dOpen = nullptr;
+    uint8_t* dFixed = nullptr;
+    Proj J{};
+    double* dAmb = nullptr;
+    double* dParts = nullptr;
+    int* dPartOff = nullptr;
+    std::vector<int> partOff;
+    int* dHoPtr = nullptr;
+    int* dHoIdx = nullptr;
+    uint8_t* dLastWriter = nullptr;
+    int* dStatus = nullptr;
+    int epoch = 0;
+    bool firstSource = true;
+    astg_solve_stats last{};
+    std::vector<void*> allocs;
+
+    template <class T>
+    T* dalloc(size_t n) {
+        void* p = nullptr;
+        ck(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)), "cudaMalloc");
+        ck(cudaMemsetAsync(p, 0, std::max<size_t>(n, 1) * sizeof(T), st), "cudaMemset");
+        allocs.push_back(p);
+        return (T*)p;
+    }
+    template <class T>
+    T* upload(const std::vector<T>& v) {
+        T* p = dalloc<T>(v.size());
+        if (!v.empty()) ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
+        return p;
+    }
+
+    ~astg_handle() {
+        if (st) cudaStreamSynchronize(st);
+        for (void* p : allocs) cudaFree(p);
+        if (J.hostDone) cudaFreeHost(J.hostDone);
+        for (cudaEvent_t e : {ev0, ev1, evA, evB})
+            if (e) cudaEventDestroy(e);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    // ---------------------------------------------------------------- host lookups
+    int get(int l, int x, int y, int z) const {
+        if (l < 0 || l >= L) return -1;
+        int r = lres[l];
+        if (x < 0 || y < 0 || z < 0 || x >= r || y >= r || z >= r) return -1;
+        return brick[l][((size_t)z * r + y) * r + x];
+    }
+    int req(int l, int x, int y, int z) const {
+        int s = get(l, x, y, z);
+        if (s < 0) {
+            char m[128];
+            snprintf(m, sizeof m, "layout: node (%d; %d, %d, %d) is missing", l, x, y, z);
+            throw std::runtime_error(m);
+        }
+        return s;
+    }
+    bool octValid(int l, int x, int y, int z) const {
+        int r = lres[l] - 1;
+        return x >= 0 && y >= 0 && z >= 0 && x < r && y < r && z < r;
+    }
+    int getUntil(int l, int x, int y, int z, bool toFinest) const {
+        int r = lres[l];
+        if (x < 0 || y < 0 || z < 0 || x >= r || y >= r || z >= r) return -1;
+        for (;;) {
+            int s = get(l, x, y, z);
+            if (s >= 0 && !(sflag[s] & SF_GHOST)) return s;
+            if (toFinest) { x <<= 1; y <<= 1; z <<= 1; l -= 1; }
+            else { x >>= 1; y >>= 1; z >>= 1; l += 1; }
+            if (l < 0 || l >= L) return -1;
+        }
+    }
+
+    // ---------------------------------------------------------------- layout
+    // OctreeLayer3 (src/octree_layer3.cpp:7-88): non-ghost cells of level l are the cells whose
+    // corner finest cell has split value l, in raster order; ghosts are their 26-neighbours of
+    // level l-1 or l+1, numbered in discovery order.
+    void buildLayout() {
+        lres.assign(L, 0); loff.assign(L, 0); lN.assign(L, 0); lG.assign(L, 0); ldh.assign(L, 0);
+        brick.assign(L, {});
+        int off = 0;
+        for (int l = 0; l < L; ++l) {
+            int r = res >> l;
+            lres[l] = r;
+            ldh[l] = dx * (1 << l);
+            loff[l] = off;
+            brick[l].assign((size_t)r * r * r, -1);
+            auto sp = [&](int x, int y, int z) { return split[((size_t)(z << l) * res + (y << l)) * res + (x << l)]; };
+            int n = 0;
+            for (int z = 0; z < r; ++z)
+                for (int y = 0; y < r; ++y)
+                    for (int x = 0; x < r; ++x)
+                        if (sp(x, y, z) == l) {
+                            brick[l][((size_t)z * r + y) * r + x] = off + n++;
+                            sx.push_back(x); sy.push_back(y); sz.push_back(z); slev.push_back(l); sflag.push_back(0);
+                        }
+            lN[l] = n;
+            int cIdx = n;
+            for (int i = 0; i < n; ++i) {
+                int bx = sx[off + i], by = sy[off + i], bz = sz[off + i];
+                for (int a = -1; a <= 1; ++a)
+                    for (int b = -1; b <= 1; ++b)
+                        for (int c = -1; c <= 1; ++c) {
+                            if (a == 0 && b == 0 && c == 0) continue;
+                            int nx = bx + a, ny = by + b, nz = bz + c;
+                            if (nx < 0 || ny < 0 || nz < 0 || nx >= r || ny >= r || nz >= r) continue;
+                            int& bk = brick[l][((size_t)nz * r + ny) * r + nx];
+                            if (bk >= 0) continue;
+                            int tv = sp(nx, ny, nz);
+                            if (tv == l - 1 || tv == l + 1) {
+                                bk = off + cIdx++;
+                                sx.push_back(nx); sy.push_back(ny); sz.push_back(nz); slev.push_back(l);
+                                sflag.push_back(SF_GHOST | (tv == l + 1 ? SF_FROM_COARSE : 0));
+                            }
+                        }
+            }
+            lG[l] = cIdx - n;
+            off += cIdx;
+        }
+        S = off;
+        // the fixed reduction tree folds at most 2048 chunk partials in one block
+        if (2LL * S > 2048LL * 2048LL) throw std::runtime_error("layout: too many cells for the reduction tree");
+    }
+
+    // OctreeVertexCenteredGrid3<TiltENode>::updateGhost (src/octree_vertex_centered_grid3.cpp:6-24)
+    void tiltGhostCopy(std::vector<HTilt>& t) {
+        for (int l = 0; l < L; ++l)
+            for (int i = lN[l]; i < lN[l] + lG[l]; ++i) {
+                int s = loff[l] + i;
+                int x = sx[s], y = sy[s], z = sz[s];
+                if (sflag[s] & SF_FROM_COARSE) {
+                    if ((x & 1) || (y & 1) || (z & 1)) continue;
+                    t[s] = t[req(l + 1, x >> 1, y >> 1, z >> 1)];
+                } else {
+                    t[s] = t[req(l - 1, x << 1, y << 1, z << 1)];
+                }
+            }
+    }
+
+    // constrainOctreeTiltE3 (src/octree_util.cpp:38-169)
+    void constrainTilts(std::vector<HTilt>& t, bool record) {
+        for (int s = 0; s < S; ++s) {  // T-joints at level transitions
+            if (sflag[s] & SF_GHOST) continue;
+            int l = slev[s], x = sx[s], y = sy[s], z = sz[s];
+            int minL = l, maxL = l;
+            for (int i = -1; i <= 0; ++i)
+                for (int j = -1; j <= 0; ++j)
+                    for (int k = -1; k <= 0; ++k) {
+                        int c = getUntil(l, x + i, y + j, z + k, true);
+                        if (c < 0) c = getUntil(l, x + i, y + j, z + k, false);
+                        // the packed-coordinate test "c > 0" of the reference skips level 0, (0,0,0)
+                        if (c >= 0 && !(slev[c] == 0 && sx[c] == 0 && sy[c] == 0 && sz[c] == 0)) {
+                            minL = std::min(minL, slev[c]);
+                            maxL = std::max(maxL, slev[c]);
+                        }
+                    }
+            if (minL < l || (maxL > l && !(x & 1) && !(y & 1) && !(z & 1))) {
+                HTilt n = t[s];
+                n.put(TF_TJOINT, true);
+                n.e = ldh[minL];
+                n.put(TF_FIXED, true);
+                n.put(TF_CLOSED, false);
+                t[s] = n;
+                if (record) tj.push_back(s);
+            }
+        }
+        for (int s = 0; s < S; ++s) {  // tilts closed by T-joints
+            if ((sflag[s] & SF_GHOST) || !t[s].has(TF_TJOINT)) continue;
+            int l = slev[s], x = sx[s], y = sy[s], z = sz[s];
+            if (t[s].e < ldh[l]) { l -= 1; x *= 2; y *= 2; z *= 2; }
+            for (int i = 0; i < 6; ++i) {
+                int q = get(l, x + OCT_NB_H[i][0], y + OCT_NB_H[i][1], z + OCT_NB_H[i][2]);
+                if (q < 0) continue;
+                HTilt n = t[q];
+                n.setE(0);
+                n.put(TF_FIXED, true);
+                n.put(TF_CLOSED_BY_T, true);
+                t[q] = n;
+            }
+        }
+        tiltGhostCopy(t);
+        for (int s = 0; s < S; ++s) {  // half tilts on coarse faces surrounded by T-joints
+            if ((sflag[s] & SF_GHOST) || !t[s].has(TF_TJOINT)) continue;
+            int l = slev[s];
+            bool coarse = t[s].e < ldh[l];
+            int ci[3] = {coarse ? sx[s] : sx[s] >> 1, coarse ? sy[s] : sy[s] >> 1, coarse ? sz[s] : sz[s] >> 1};
+            int lc = l + (!coarse);
+            for (int axis = 0; axis < 3; ++axis) {
+                if (ci[axis] == 0 || ci[axis] == lres[l - coarse] - 1) continue;
+                bool flag = true;
+                for (int i = 0; i <= 1 && flag; ++i)
+                    for (int j = 0; j <= 1 && flag; ++j) {
+                        if (i == 0 && j == 0) continue;
+                        int id[3] = {ci[0], ci[1], ci[2]};
+                        id[(axis + 1) % 3] += i;
+                        id[(axis + 2) % 3] += j;
+                        int c = lc < L ? getUntil(lc, id[0], id[1], id[2], true) : -1;
+                        if (c < 0 && lc < L) c = getUntil(lc, id[0], id[1], id[2], false);
+                        if (c < 0 || !t[c].has(TF_TJOINT)) flag = false;
+                    }
+                if (flag) {
+                    int nb[3] = {ci[0], ci[1], ci[2]};
+                    nb[axis] -= 1;
+                    int c = lc < L ? getUntil(lc, ci[0], ci[1], ci[2], true) : -1;
+                    int c1 = lc < L ? getUntil(lc, nb[0], nb[1], nb[2], true) : -1;
+                    int lvc = c >= 0 ? slev[c] : 15;  // UNPACK_LEVEL3(-1)
+                    if (c1 < 0 || lvc == slev[c1]) flag = false;
+                }
+                if (!flag) continue;
+                int id[3] = {ci[0] * 2, ci[1] * 2, ci[2] * 2};
+                id[(axis + 1) % 3] += 1;
+                id[(axis + 2) % 3] += 1;
+                int hl = l - coarse;
+                int hs = get(hl, id[0], id[1], id[2]);
+                if (hs < 0) continue;
+                HTilt n = t[hs];
+                n.put(TF_CLOSED, true);
+                n.put(TF_HALF, true);
+                n.put(TF_FIXED, true);
+                n.dir = axis + (coarse ? 3 : 0);
+                n.e = ldh[hl];
+                t[hs] = n;
+                if (record) half.push_back(hs);
+                int tp[3] = {id[0], id[1], id[2]};
+                tp[axis] += n.dir < 3 ? 1 : -1;
+                int ts = req(hl, tp[0], tp[1], tp[2]);
+                if (record && std::find(cbh.begin(), cbh.end(), ts) == cbh.end()) cbh.push_back(ts);
+                HTilt m = t[ts];
+                m.setE(0);
+                m.put(TF_CLOSED_BY_T, true);
+                m.dir = -1;
+                m.put(TF_FIXED, true);
+                t[ts] = m;
+            }
+        }
+    }
+
+    // Constants::init least-squares tables (src/constants.cpp:170-256), inverted through a
+    // partial-pivoting LU in the order Eigen's MatrixXd::inverse() uses
+    void buildTables() {
+        M37.assign(128 * 21, 0.0);
+        const double s = INV_SQRT3;
+        const double rows[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {s, s, s}, {-s, s, s}, {-s, -s, s}, {s, -s, s}};
+        for (int bits = 0; bits < 128; ++bits) {
+            int use[7], cnt = 0;
+            for (int k = 0; k < 7; ++k) { use[k] = (bits >> (6 - k)) & 1; cnt += use[k]; }
+            if (cnt <= 1) continue;
+            double G[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            for (int r = 0; r < 7; ++r)
+                if (use[r])
+                    for (int i = 0; i < 3; ++i)
+                        for (int j = 0; j < 3; ++j) G[i][j] += rows[r][i] * rows[r][j];
+            double lu[3][3];
+            memcpy(lu, G, sizeof lu);
+            int tr[3];
+            for (int k = 0; k < 3; ++k) {
+                int piv = k;
+                double best = std::fabs(lu[k][k]);
+                for (int i = k + 1; i < 3; ++i)
+                    if (std::fabs(lu[i][k]) > best) { best = std::fabs(lu[i][k]); piv = i; }
+                tr[k] = piv;
+                if (best != 0) {
+                    if (piv != k)
+                        for (int j = 0; j < 3; ++j) std::swap(lu[k][j], lu[piv][j]);
+                    for (int i = k + 1; i < 3; ++i) lu[i][k] /= lu[k][k];
+                }
+                for (int i = k + 1; i < 3; ++i)
+                    for (int j = k + 1; j < 3; ++j) lu[i][j] -= lu[i][k] * lu[k][j];
+            }
+            double inv[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+            for (int k = 0; k < 3; ++k)
+                if (tr[k] != k)
+                    for (int j = 0; j < 3; ++j) std::swap(inv[k][j], inv[tr[k]][j]);
+            for (int i = 0; i < 3; ++i)
+                for (int r2 = i + 1; r2 < 3; ++r2)
+                    for (int j = 0; j < 3; ++j) inv[r2][j] -= inv[i][j] * lu[r2][i];
+            for (int i = 2; i >= 0; --i) {
+                double rcp = 1.0 / lu[i][i];
+                for (int j = 0; j < 3; ++j) inv[i][j] *= rcp;
+                for (int r2 = 0; r2 < i; ++r2)
+                    for (int j = 0; j < 3; ++j) inv[r2][j] -= inv[i][j] * lu[r2][i];
+            }
+            for (int k = 0; k < 3; ++k)
+                for (int r = 0; r < 7; ++r)
+                    if (use[r]) M37[(size_t)bits * 21 + k * 7 + r] = inv[k][0] * rows[r][0] + inv[k][1] * rows[r][1] + inv[k][2] * rows[r][2];
+        }
+    }
+
+    V3 vertPos(int s) const { double h = ldh[slev[s]]; return v3(sx[s] * h, sy[s] * h, sz[s] * h); }
+    V3 macPos(int a, int s) const {
+        double h = ldh[slev[s]];
+        double p[3] = {sx[s] * h + 0.5 * h, sy[s] * h + 0.5 * h, sz[s] * h + 0.5 * h};
+        int c[3] = {sx[s], sy[s], sz[s]};
+        p[a] = c[a] * h + 0.0 * h;
+        return v3(p[0], p[1], p[2]);
+    }
+    static V3 tiltPos(V3 c, int dir, double e) {
+        int m = dir & 3;
+        double tz = (dir < 4 ? 1 : -1) * e / 3.0;
+        double ty = (m < 2 ? 1 : -1) * e / 3.0;
+        double tx = ((m == 0 || m == 3) ? 1 : -1) * e / 3.0;
+        return v3(c.x + tx, c.y + ty, c.z + tz);
+    }
+
+    // ---------------------------------------------------------------- initialisation
+    void init(const astg_params& p, const int32_t* splitMap) {
+        P = p;
+        if (P.levels < 2 || P.levels > MAXL || P.coarsest < 4) throw std::invalid_argument("levels must be 2..6, coarsest >= 4");
+        L = P.levels;
+        res = P.coarsest << (L - 1);
+        dx = 1.0 / res;
+        if (splitMap) split.assign(splitMap, splitMap + (size_t)res * res * res);
+        else split = astg_scene::split_map(res, L, astg_scene::Sphere{P.src_x, P.src_y, P.src_z, P.src_r});
+        for (int32_t v : split)
+            if (v < 0 || v >= L) throw std::invalid_argument("split map holds a level outside [0, levels)");
+        ck(cudaSetDevice(P.device), "cudaSetDevice");
+        ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+        for (cudaEvent_t* e : {&ev0, &ev1, &evA, &evB}) ck(cudaEventCreate(e), "event");
+
+        buildLayout();
+        buildTables();
+        for (int b = 0; b < 2; ++b) te[b].assign(S, HTilt());
+        tOpen.assign(S, 0);
+        tFixed.assign(S, 0);
+        constrainTilts(te[0], true);
+        tiltGhostCopy(te[0]);
+        constrainTilts(te[1], false);
+        tiltGhostCopy(te[1]);
+        H = (int)half.size();
+        {
+            std::vector<int> hs = half;
+            std::sort(hs.begin(), hs.end());
+            if (std::adjacent_find(hs.begin(), hs.end()) != hs.end())
+                throw std::runtime_error("layout: a half tilt was recorded twice");
+        }
+        // fixed and outermost tilts (src/octree_omnigrid_solver3.cpp:128-145)
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & SF_GHOST) continue;
+            HTilt n = te[0][s];
+            if (n.has(TF_TJOINT) || n.has(TF_FIXED)) {
+                tOpen[s] = !n.has(TF_CLOSED);
+                tFixed[s] = 1;
+                continue;
+            }
+            int r = lres[slev[s]];
+            if (sx[s] == 0 || sy[s] == 0 || sz[s] == 0 || sx[s] == r - 1 || sy[s] == r - 1 || sz[s] == r - 1) {
+                n.setE(0);
+                n.put(TF_FIXED, true);
+                tOpen[s] = !n.has(TF_CLOSED);
+                tFixed[s] = 1;
+                te[0][s] = n;
+                te[1][s] = n;
+            }
+        }
+        // cut-cell weights of a collider-free domain (src/octree_omnigrid_solver3.cpp:1169-1238)
+        wMac.assign((size_t)3 * S, 1.0);
+        wTilt.assign((size_t)8 * S, 1.0);
+        for (int hs : half) {
+            double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            int dir = te[0][hs].dir, l = slev[hs];
+            int id[3] = {sx[hs] >> 1, sy[hs] >> 1, sz[hs] >> 1};
+            id[dir % 3] -= dir < 3 ? 1 : 0;
+            if (l + 1 < L && octValid(l + 1, id[0], id[1], id[2])) w[HALF_SLOT_H[dir][4]] = 1.0;
+            for (int i = 0; i < 4; ++i) {
+                int k = HALF_SLOT_H[dir][i];
+                if (octValid(l, sx[hs] + TILT_NB_OCT_H[k][0], sy[hs] + TILT_NB_OCT_H[k][1], sz[hs] + TILT_NB_OCT_H[k][2])) w[k] = 1.0;
+            }
+            for (int k = 0; k < 8; ++k) wTilt[(size_t)hs * 8 + k] = w[k];
+        }
+        uploadAll();
+    }
+
+    void uploadAll() {
+        // finest non-ghost level containing each finest cell (OctreeGridLayout3::levelCoordinate)
+        std::vector<uint8_t> locate((size_t)res * res * res, 0xff);
+        for (int z = 0; z < res; ++z)
+            for (int y = 0; y < res; ++y)
+                for (int x = 0; x < res; ++x) {
+                    for (int l = 0; l < L; ++l) {
+                        int s = get(l, x >> l, y >> l, z >> l);
+                        if (s >= 0 && !(sflag[s] & SF_GHOST)) { locate[((size_t)z * res + y) * res + x] = (uint8_t)l; break; }
+                    }
+                }
+        std::vector<int4> slot(S);
+        for (int s = 0; s < S; ++s) slot[s] = make_int4(sx[s], sy[s], sz[s], slev[s] | (sflag[s] << 8));
+        std::vector<uint8_t> halfMark(S, 0);
+        for (int hs : half) halfMark[hs] = 1;
+        // half tilts facing each coarse octagon, in list order (assembly, :572-581)
+        std::vector<int> hoCnt(S + 1, 0), hoIdx;
+        std::vector<std::vector<int>> ho(S);
+        for (int i = 0; i < H; ++i) {
+            int hs = half[i];
+            int dir = te[0][hs].dir, l = slev[hs];
+            int id[3] = {sx[hs] >> 1, sy[hs] >> 1, sz[hs] >> 1};
+            id[dir % 3] -= dir < 3 ? 1 : 0;
+            if (l + 1 < L && octValid(l + 1, id[0], id[1], id[2])) ho[req(l + 1, id[0], id[1], id[2])].push_back(i);
+        }
+        std::vector<int> hoPtr(S + 1, 0);
+        for (int s = 0; s < S; ++s) {
+            hoPtr[s + 1] = hoPtr[s] + (int)ho[s].size();
+            hoIdx.insert(hoIdx.end(), ho[s].begin(), ho[s].end());
+        }
+        // only the last half tilt of the list that targets a MAC face writes it
+        // (updateGhostFromHalfTilt, src/octree_omni_face_centered_grid3.cpp:162-173)
+        std::vector<uint8_t> lastWriter(std::max(H, 1), 0);
+        {
+            std::vector<long long> seen;
+            for (int i = H - 1; i >= 0; --i) {
+                int hs = half[i];
+                int a = te[0][hs].dir % 3;
+                int t = req(slev[hs] + 1, sx[hs] >> 1, sy[hs] >> 1, sz[hs] >> 1);
+                long long key = (long long)t * 3 + a;
+                if (std::find(seen.begin(), seen.end(), key) == seen.end()) { lastWriter[i] = 1; seen.push_back(key); }
+            }
+        }
+        d.L = L; d.res = res; d.S = S; d.H = H; d.nTJ = (int)tj.size(); d.nCBH = (int)cbh.size();
+        d.dx = dx;
+        for (int l = 0; l < L; ++l) {
+            d.lres[l] = lres[l]; d.loff[l] = loff[l]; d.lN[l] = lN[l]; d.lG[l] = lG[l]; d.ldh[l] = ldh[l];
+            d.brick[l] = upload(brick[l]);
+        }
+        d.locate = upload(locate);
+        d.slot = upload(slot);
+        d.half = upload(half);
+        d.halfMark = upload(halfMark);
+        d.tj = upload(tj);
+        d.cbh = upload(cbh);
+        d.wMac = upload(wMac);
+        d.wTilt = upload(wTilt);
+        d.M37 = upload(M37);
+        dStatus = dalloc<int>(1);
+        d.status = dStatus;
+        d.buoyD = P.buoy_density; d.buoyT = P.buoy_temp; d.rho = P.rho; d.decay = P.decay;
+        d.closedMask = P.closed_mask;
+        d.srcX = P.src_x; d.srcY = P.src_y; d.srcZ = P.src_z; d.srcR = P.src_r;
+        dHoPtr = upload(hoPtr);
+        dHoIdx = upload(hoIdx);
+        dLastWriter = upload(lastWriter);
+        // fields
+        for (int b = 0; b < 2; ++b) {
+            F[b].dO = dalloc<double>(S); F[b].dT = dalloc<double>(S);
+            F[b].hO = dalloc<double>(S); F[b].hT = dalloc<double>(S);
+            F[b].mac = dalloc<double>((size_t)3 * S);
+            F[b].tv = dalloc<double>((size_t)8 * S);
+            F[b].dualO = dalloc<double>((size_t)3 * S);
+            F[b].dualT = dalloc<double>((size_t)3 * S);
+            std::vector<double> e(S);
+            std::vector<uint32_t> f(S);
+            for (int s = 0; s < S; ++s) { e[s] = te[b][s].e; f[s] = te[b][s].packed(); }
+            F[b].te = upload(e);
+            F[b].tf = upload(f);
+        }
+        dOpen = upload(tOpen);
+        dFixed = upload(tFixed);
+        // initial velocity: seeded curl noise on valid MAC faces, open tilts and half tilts
+        {
+            astg_scene::CurlNoise cn(P.seed, P.noise);
+            std::vector<double> mac((size_t)3 * S, 0.0), tv((size_t)8 * S, 0.0);
+            auto vel = [&](V3 p) {
+                double pp[3] = {p.x, p.y, p.z}, u[3];
+                cn.velocity(pp, u);
+                return v3(u[0], u[1], u[2]);
+            };
+            for (int s = 0; s < S; ++s) {
+                if (sflag[s] & SF_GHOST) continue;
+                int l = slev[s], r = lres[l];
+                for (int a = 0; a < 3; ++a) {
+                    int c[3] = {sx[s], sy[s], sz[s]};
+                    bool ok = true;
+                    for (int k = 0; k < 3; ++k) ok &= c[k] >= 0 && c[k] < (k == a ? r : r - 1);
+                    if (!ok) continue;
+                    mac[(size_t)a * S + s] = comp(vel(macPos(a, s)), a);
+                }
+                if (tOpen[s]) {
+                    for (int k = 0; k < 8; ++k) {
+                        V3 u = vel(tiltPos(vertPos(s), k, te[0][s].e));
+                        V3 dn = v3(TILT_UP_SIGN_H[k][0] * INV_SQRT3, TILT_UP_SIGN_H[k][1] * INV_SQRT3, TILT_UP_SIGN_H[k][2] * INV_SQRT3);
+                        tv[(size_t)s * 8 + k] = u.x * dn.x + u.y * dn.y + u.z * dn.z;
+                    }
+                }
+            }
+            for (int hs : half) {
+                int dir = te[0][hs].dir;
+                double nv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                for (int i = 0; i < 5; ++i) {
+                    int k = HALF_SLOT_H[dir][i];
+                    V3 p = (i == 4) ? vertPos(hs) : tiltPos(vertPos(hs), k, te[0][hs].e);
+                    V3 u = vel(p);
+                    V3 dn = (i == 4) ? v3(HALF_DIR_POS_H[k][0], HALF_DIR_POS_H[k][1], HALF_DIR_POS_H[k][2])
+                                     : v3(TILT_UP_SIGN_H[k][0] * INV_SQRT3, TILT_UP_SIGN_H[k][1] * INV_SQRT3, TILT_UP_SIGN_H[k][2] * INV_SQRT3);
+                    nv[k] = u.x * dn.x + u.y * dn.y + u.z * dn.z;
+                }
+                for (int k = 0; k < 8; ++k) tv[(size_t)hs * 8 + k] = nv[k];
+            }
+            ck(cudaMemcpyAsync(F[0].mac, mac.data(), mac.size() * 8, cudaMemcpyHostToDevice, st), "upload mac");
+            ck(cudaMemcpyAsync(F[0].tv, tv.data(), tv.size() * 8, cudaMemcpyHostToDevice, st), "upload tilt");
+        }
+        // mean temperature partials
+        partOff.assign(L + 1, 0);
+        for (int l = 0; l < L; ++l) partOff[l + 1] = partOff[l] + (lN[l] + lG[l] + 2047) / 2048;
+        dParts = dalloc<double>(partOff[L] + 1);
+        dPartOff = upload(partOff);
+        dAmb = dalloc<double>(1);
+        allocProj();
+        ck(cudaStreamSynchronize(st), "init");
+    }
+
+    void allocProj() {
+        long long rows = (long long)S + H;
+        J.cnt = dalloc<int>(S);
+        J.base = dalloc<int>(S);
+        J.bsum = dalloc<int>((rows + 1023) / 1024 + 1);
+        J.n0 = dalloc<int>(1);
+        J.nDof = dalloc<int>(1);
+        J.nnz = dalloc<int>(1);
+        J.pO = dalloc<int>(S);
+        J.pT = dalloc<int>(S);
+        J.rowCnt = dalloc<int>(rows);
+        J.rowPtr = dalloc<int>(rows + 1);
+        J.padCol = dalloc<int>(rows * ROW_W);
+        J.padVal = dalloc<double>(rows * ROW_W);
+        J.bRaw = dalloc<double>(rows);
+        J.col = dalloc<int>(rows * ROW_W);
+        J.val = dalloc<double>(rows * ROW_W);
+        J.diagPos = dalloc<int>(rows);
+        J.tpos = dalloc<int>(rows * ROW_W);
+        J.b = dalloc<double>(rows);
+        J.Lv = dalloc<double>(rows * ROW_W);
+        J.invdiag = dalloc<double>(rows);
+        J.adiag = dalloc<double>(rows);
+        J.ready = dalloc<int>(rows);
+        J.counter = dalloc<int>(1);
+        int sms = 0;
+        ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P.device), "attr");
+        J.sweepBlocks = std::max(1, sms) * 8;
+        J.x = dalloc<double>(rows);
+        J.r = dalloc<double>(rows);
+        J.s = dalloc<double>(rows);
+        J.z = dalloc<double>(rows);
+        J.part = dalloc<double>((rows + 2047) / 2048 + 1);
+        J.sc = dalloc<double>(SC_COUNT);
+        J.isc = dalloc<int>(ISC_COUNT);
+        J.amax = dalloc<unsigned long long>(1);
+        J.done = dalloc<int>(1);
+        ck(cudaMallocHost(&J.hostDone, sizeof(int)), "cudaMallocHost");
+        *J.hostDone = 0;
+    }
+
+    // ---------------------------------------------------------------- step
+    void checkStatus() {
+        int s = 0;
+        ck(cudaMemcpyAsync(&s, dStatus, sizeof(int), cudaMemcpyDeviceToHost, st), "status");
+        ck(cudaStreamSynchronize(st), "sync");
+        if (s != DS_OK) {
+            int zero = 0;
+            ck(cudaMemcpy(dStatus, &zero, sizeof(int), cudaMemcpyHostToDevice), "status reset");
+            if (s == DS_WAIT_TIMEOUT) throw std::runtime_error("device wait timed out (status 3)");
+            throw std::runtime_error("layout lookup failed on the device (status " + std::to_string(s) + ")");
+        }
+    }
+
+    void project(double dt) {
+        Fields& C = F[cur];
+        launch_dof_numbering(d, dOpen, J, st);
+        launch_assemble(d, C, dOpen, J, dHoPtr, dHoIdx, dt, st);
+        launch_factor(d, J, P.omega, P.min_diag, epoch, st);
+        ck(cudaEventRecord(evA, st), "event");
+        launch_pcg_fp64(d, J, P.tol, P.max_iter, epoch, 8, st);
+        ck(cudaEventRecord(evB, st), "event");
+        launch_pressure_update(d, C, dOpen, J.pO, J.pT, J.x, dt, st);
+        // statistics of the solve
+        int isc[ISC_COUNT], n = 0, nnz = 0;
+        double sc[SC_COUNT];
+        ck(cudaMemcpyAsync(isc, J.isc, sizeof isc, cudaMemcpyDeviceToHost, st), "stats");
+        ck(cudaMemcpyAsync(sc, J.sc, sizeof sc, cudaMemcpyDeviceToHost, st), "stats");
+        ck(cudaMemcpyAsync(&n, J.nDof, sizeof n, cudaMemcpyDeviceToHost, st), "stats");
+        ck(cudaMemcpyAsync(&nnz, J.nnz, sizeof nnz, cudaMemcpyDeviceToHost, st), "stats");
+        ck(cudaStreamSynchronize(st), "project");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, evA, evB);
+        last.iterations = isc[ISC_ITERS];
+        last.converged = isc[ISC_CONVERGED];
+        last.outer = 0;
+        last.n = n;
+        last.nnz = nnz;
+        last.residual = sc[SC_RESID];
+        last.tolerance = sc[SC_TOL];
+        last.ms = ms;
+    }
+
+    void stage(int id, double dt) {
+        Fields& C = F[cur];
+        Fields& N = F[1 - cur];
+        switch (id) {
+            case 0:
+                if (P.src_r > 0) launch_source(d, C, st);
+                if (firstSource) {
+                    launch_scalar_ghost(d, C.dO, C.dT, C.te, C.tf, st);
+                    launch_scalar_ghost(d, C.hO, C.hT, C.te, C.tf, st);
+                    firstSource = false;
+                }
+                break;
+            case 1:
+                launch_mean_temperature(d, C.hO, dParts, dPartOff, partOff.data(), dAmb, st);
+                launch_force(d, C, dOpen, dAmb, dt, st);
+                break;
+            case 2: launch_walls_and_ghost(d, C, dLastWriter, st); break;
+            case 3: project(dt); break;
+            case 4:
+                launch_walls_and_ghost(d, C, dLastWriter, st);
+                launch_dual(d, C, st);
+                break;
+            case 5:
+                if (P.tilt_adaptivity) launch_adjust(d, C, N, dOpen, dFixed, dt, st);
+                launch_advect_scalars(d, C, N, dOpen, dt, st);
+                launch_advect_velocity(d, C, N, dt, st);
+                cur = 1 - cur;
+                launch_decay(d, F[cur], st);
+                break;
+            default: throw std::invalid_argument("stage must be 0..5");
+        }
+        ck(cudaGetLastError(), "launch");
+    }
+
+    void step(double dt, astg_step_stats* out) {
+        ck(cudaEventRecord(ev0, st), "event");
+        for (int i = 0; i < 6; ++i) stage(i, dt);
+        ck(cudaEventRecord(ev1, st), "event");
+        checkStatus();
+        if (out) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev0, ev1);
+            out->solve = last;
+            out->ms_total = ms;
+            out->ms_project = last.ms;
+            out->ms_force = 0;
+            out->ms_advect = 0;
+        }
+    }
+
+    // ---------------------------------------------------------------- array exchange
+    // "t_<field>" addresses the swap partner of a double-buffered state array
+    static bool isPartner(const std::string& n) {
+        static const char* fields[] = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel",
+                                       "dual_oct", "dual_tilt", "tilt_e", "tilt_flags", "tilt_open"};
+        if (n.compare(0, 2, "t_") != 0) return false;
+        for (const char* f : fields)
+            if (n.compare(2, std::string::npos, f) == 0) return true;
+        return false;
+    }
+    template <class T>
+    void down(const T* src, void* dst, size_t n) {
+        ck(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, st), "download");
+        ck(cudaStreamSynchronize(st), "download");
+    }
+    template <class T>
+    void up(T* dst, const void* src, size_t n) {
+        ck(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaStreamSynchronize(st), "upload");
+    }
+    int lastN() {
+        int n = 0;
+        down(J.nDof, &n, 1);
+        return n;
+    }
+
+    // returns the byte size of a named array; copies it out when dst != nullptr
+    size_t getArray(const std::string& name0, void* dst, size_t bytes) {
+        std::string name = name0;
+        int b = cur;
+        if (isPartner(name)) { b = 1 - cur; name = name.substr(2); }
+        Fields& G = F[b];
+        auto need = [&](size_t nb) {
+            if (dst && bytes != nb) throw std::invalid_argument("astg_get " + name0 + ": expected " + std::to_string(nb) + " bytes");
+            return nb;
+        };
+        if (name == "density_oct") { size_t nb = need(8 * (size_t)S); if (dst) down(G.dO, dst, S); return nb; }
+        if (name == "density_tilt") { size_t nb = need(8 * (size_t)S); if (dst) down(G.dT, dst, S); return nb; }
+        if (name == "heat_oct") { size_t nb = need(8 * (size_t)S); if (dst) down(G.hO, dst, S); return nb; }
+        if (name == "heat_tilt") { size_t nb = need(8 * (size_t)S); if (dst) down(G.hT, dst, S); return nb; }
+        if (name == "mac") { size_t nb = need(24 * (size_t)S); if (dst) down(G.mac, dst, 3 * (size_t)S); return nb; }
+        if (name == "tilt_vel") { size_t nb = need(64 * (size_t)S); if (dst) down(G.tv, dst, 8 * (size_t)S); return nb; }
+        if (name == "dual_oct") { size_t nb = need(24 * (size_t)S); if (dst) down(G.dualO, dst, 3 * (size_t)S); return nb; }
+        if (name == "dual_tilt") { size_t nb = need(24 * (size_t)S); if (dst) down(G.dualT, dst, 3 * (size_t)S); return nb; }
+        if (name == "tilt_e") { size_t nb = need(8 * (size_t)S); if (dst) down(G.te, dst, S); return nb; }
+        if (name == "tilt_flags") {
+            size_t nb = need(8 * (size_t)S);
+            if (dst) {
+                std::vector<uint32_t> f(S);
+                down(G.tf, f.data(), S);
+                int32_t* o = (int32_t*)dst;
+                for (int s = 0; s < S; ++s) { o[2 * s] = (int32_t)(f[s] & 0xff); o[2 * s + 1] = tf_dir(f[s]); }
+            }
+            return nb;
+        }
+        if (name == "tilt_open") {
+            size_t nb = need((size_t)S);
+            if (dst) {
+                std::vector<uint8_t> o(S), fx(S);
+                down(dOpen, o.data(), S);
+                down(dFixed, fx.data(), S);
+                uint8_t* q = (uint8_t*)dst;
+                for (int s = 0; s < S; ++s) q[s] = (o[s] ? 1 : 0) | (fx[s] ? 2 : 0);
+            }
+            return nb;
+        }
+        if (b != cur) throw std::invalid_argument("astg_get: no swap partner for " + name);
+        if (name == "slot_coords") {
+            size_t nb = need(16 * (size_t)S);
+            if (dst) {
+                int32_t* o = (int32_t*)dst;
+                for (int s = 0; s < S; ++s) {
+                    o[4 * s] = sx[s]; o[4 * s + 1] = sy[s]; o[4 * s + 2] = sz[s];
+                    // reference flags: VALID | IS_GHOST | GHOST_FROM_COARSE
+                    o[4 * s + 3] = 1 | ((sflag[s] & SF_GHOST) ? 2 : 0) | ((sflag[s] & SF_FROM_COARSE) ? 4 : 0);
+                }
+            }
+            return nb;
+        }
+        if (name == "level_sizes") {
+            size_t nb = need(12 * (size_t)L);
+            if (dst) {
+                int32_t* o = (int32_t*)dst;
+                for (int l = 0; l < L; ++l) { o[3 * l] = lN[l]; o[3 * l + 1] = lG[l]; o[3 * l + 2] = lN[l] + lG[l]; }
+            }
+            return nb;
+        }
+        if (name == "split_map") { size_t nb = need(4 * split.size()); if (dst) memcpy(dst, split.data(), nb); return nb; }
+        if (name == "half_tilts" || name == "t_joints" || name == "closed_by_half_tilt") {
+            const std::vector<int>& v = name == "half_tilts" ? half : (name == "t_joints" ? tj : cbh);
+            std::vector<long long> o;
+            for (int q : v) o.push_back(((long long)slev[q] << 60) | ((long long)sx[q] << 40) | ((long long)sy[q] << 20) | (long long)sz[q]);
+            if (name == "t_joints") std::sort(o.begin(), o.end());
+            size_t nb = need(8 * o.size());
+            if (dst && nb) memcpy(dst, o.data(), nb);
+            return nb;
+        }
+        if (name == "w_mac") { size_t nb = need(8 * wMac.size()); if (dst) memcpy(dst, wMac.data(), nb); return nb; }
+        if (name == "w_tilt") { size_t nb = need(8 * wTilt.size()); if (dst) memcpy(dst, wTilt.data(), nb); return nb; }
+        if (name == "dual_tables") { size_t nb = need(8 * M37.size()); if (dst) memcpy(dst, M37.data(), nb); return nb; }
+        if (name == "pindex_oct") { size_t nb = need(4 * (size_t)S); if (dst) down(J.pO, dst, S); return nb; }
+        if (name == "pindex_tilt") { size_t nb = need(4 * (size_t)S); if (dst) down(J.pT, dst, S); return nb; }
+        if (name == "A_rowptr") { int n = lastN(); size_t nb = need(4 * (size_t)(n + 1)); if (dst) down(J.rowPtr, dst, n + 1); return nb; }
+        if (name == "A_col" || name == "A_val") {
+            int n = lastN(), nnz = 0;
+            down(J.nnz, &nnz, 1);
+            (void)n;
+            size_t nb = need((name == "A_col" ? 4 : 8) * (size_t)nnz);
+            if (dst) {
+                if (name == "A_col") down(J.col, dst, nnz);
+                else down(J.val, dst, nnz);
+            }
+            return nb;
+        }
+        if (name == "b") { int n = lastN(); size_t nb = need(8 * (size_t)n); if (dst) down(J.b, dst, n); return nb; }
+        if (name == "p") { int n = lastN(); size_t nb = need(8 * (size_t)n); if (dst) down(J.x, dst, n); return nb; }
+        if (name == "pcg_iters") {
+            size_t nb = need(8);
+            if (dst) {
+                int32_t* o = (int32_t*)dst;
+                o[0] = last.iterations;
+                o[1] = last.converged;
+            }
+            return nb;
+        }
+        if (name == "ambT") { size_t nb = need(8); if (dst) down(dAmb, dst, 1); return nb; }
+        throw std::invalid_argument("astg_get: unknown array " + name0);
+    }
+
+    void setArray(const std::string& name0, const void* src, size_t bytes) {
+        std::string name = name0;
+        int b = cur;
+        if (isPartner(name)) { b = 1 - cur; name = name.substr(2); }
+        Fields& G = F[b];
+        auto need = [&](size_t nb) {
+            if (bytes != nb) throw std::invalid_argument("astg_set " + name0 + ": expected " + std::to_string(nb) + " bytes");
+        };
+        if (name == "density_oct") { need(8 * (size_t)S); up(G.dO, src, S); return; }
+        if (name == "density_tilt") { need(8 * (size_t)S); up(G.dT, src, S); return; }
+        if (name == "heat_oct") { need(8 * (size_t)S); up(G.hO, src, S); return; }
+        if (name == "heat_tilt") { need(8 * (size_t)S); up(G.hT, src, S); return; }
+        if (name == "mac") { need(24 * (size_t)S); up(G.mac, src, 3 * (size_t)S); return; }
+        if (name == "tilt_vel") { need(64 * (size_t)S); up(G.tv, src, 8 * (size_t)S); return; }
+        if (name == "dual_oct") { need(24 * (size_t)S); up(G.dualO, src, 3 * (size_t)S); return; }
+        if (name == "dual_tilt") { need(24 * (size_t)S); up(G.dualT, src, 3 * (size_t)S); return; }
+        if (name == "tilt_e") { need(8 * (size_t)S); up(G.te, src, S); return; }
+        if (name == "tilt_flags") {
+            need(8 * (size_t)S);
+            const int32_t* f = (const int32_t*)src;
+            std::vector<uint32_t> v(S);
+            for (int s = 0; s < S; ++s) v[s] = ((uint32_t)f[2 * s] & 0xff) | ((uint32_t)(f[2 * s + 1] + 1) << 8);
+            up(G.tf, v.data(), S);
+            return;
+        }
+        if (name == "tilt_open") {
+            need((size_t)S);
+            const uint8_t* q = (const uint8_t*)src;
+            std::vector<uint8_t> o(S), fx(S);
+            for (int s = 0; s < S; ++s) { o[s] = q[s] & 1; fx[s] = (q[s] >> 1) & 1; }
+            up(dOpen, o.data(), S);
+            up(dFixed, fx.data(), S);
+            return;
+        }
+        throw std::invalid_argument("astg_set: unknown or read-only array " + name0);
+    }
+};
+
+// ==================================================================== C ABI
+namespace {
+astg_status fail(astg_handle* h, const std::exception& e, astg_status code) {
+    if (h) h->err = e.what();
+    return code;
+}
+template <class F>
+astg_status guard(astg_handle* h, F&& f) {
+    if (!h) return ASTG_BAD_ARG;
+    try {
+        f();
+        return ASTG_OK;
+    } catch (CudaError& e) {
+        return fail(h, e, ASTG_CUDA_ERROR);
+    } catch (std::invalid_argument& e) {
+        return fail(h, e, ASTG_BAD_ARG);
+    } catch (std::runtime_error& e) {
+        std::string m = e.what();
+        if (m.find("timed out") != std::string::npos) return fail(h, e, ASTG_DEVICE_WAIT_TIMEOUT);
+        if (m.find("layout") != std::string::npos) return fail(h, e, ASTG_LAYOUT_ERROR);
+        return fail(h, e, ASTG_CUDA_ERROR);
+    } catch (std::exception& e) {
+        return fail(h, e, ASTG_CUDA_ERROR);
+    }
+}
+}  // namespace
+
+extern "C" {
+
+void astg_default_params(astg_params* p, int coarsest, int levels) {
+    if (!p) return;
+    memset(p, 0, sizeof *p);
+    p->coarsest = coarsest;
+    p->levels = levels;
+    p->tol = 1e-6;
+    p->max_iter = 3000;
+    p->omega = 0.97;
+    p->min_diag = 0.25;
+    p->rho = 2.0;
+    p->buoy_density = -0.1;
+    p->buoy_temp = 1.0;
+    p->decay = 1.0;
+    p->closed_mask = 1 | 2 | 4 | 8 | 32;
+    p->tilt_adaptivity = 1;
+    astg_scene::Sphere s = astg_scene::default_source();
+    p->src_x = s.cx; p->src_y = s.cy; p->src_z = s.cz; p->src_r = s.r;
+    p->noise = 1e-3;
+    p->seed = 0;
+    p->precision = ASTG_FP64;
+    p->device = 0;
+}
+
+astg_status astg_create(const astg_params* p, const int32_t* split_map, astg_handle** out) {
+    if (!p || !out) return ASTG_BAD_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return ASTG_NO_DEVICE;
+    auto* h = new astg_handle();
+    astg_status s = guard(h, [&] { h->init(*p, split_map); });
+    if (s != ASTG_OK) {
+        // keep the handle so the caller can read the message; it must still be destroyed
+        *out = h;
+        return s;
+    }
+    *out = h;
+    return ASTG_OK;
+}
+
+void astg_destroy(astg_handle* h) { delete h; }
+
+const char* astg_last_error(const astg_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+astg_status astg_step(astg_handle* h, double dt, astg_step_stats* stats) {
+    if (!(dt > 0)) return ASTG_BAD_ARG;
+    astg_status s = guard(h, [&] { h->step(dt, stats); });
+    if (s == ASTG_OK && h->last.converged == 0) return ASTG_NOT_CONVERGED;
+    return s;
+}
+
+astg_status astg_stage(astg_handle* h, int stage, double dt) {
+    return guard(h, [&] {
+        h->stage(stage, dt);
+        h->checkStatus();
+    });
+}
+
+astg_status astg_set_solver_parameters(astg_handle* h, double tol, int max_iter, double omega, double min_diag) {
+    if (!h || max_iter <= 0) return ASTG_BAD_ARG;
+    h->P.tol = tol < 1e-30 ? 1e-30 : tol;
+    h->P.max_iter = max_iter;
+    h->P.omega = omega;
+    h->P.min_diag = min_diag;
+    return ASTG_OK;
+}
+
+astg_status astg_set_precision(astg_handle* h, astg_precision prec) {
+    if (!h || (prec != ASTG_FP64 && prec != ASTG_MIXED)) return ASTG_BAD_ARG;
+    h->P.precision = prec;
+    return ASTG_OK;
+}
+
+astg_status astg_last_solve(const astg_handle* h, astg_solve_stats* out) {
+    if (!h || !out) return ASTG_BAD_ARG;
+    *out = h->last;
+    return ASTG_OK;
+}
+
+long long astg_size(const astg_handle* h, int what) {
+    if (!h) return -1;
+    switch (what) {
+        case 0: return h->S;
+        case 1: return h->L;
+        case 2: return h->res;
+        case 3: return h->last.n;
+        case 4: return h->H;
+        case 5: return h->last.nnz;
+        default: return -1;
+    }
+}
+
+astg_status astg_get(astg_handle* h, const char* name, void* dst, size_t bytes, size_t* bytes_needed) {
+    if (!h || !name) return ASTG_BAD_ARG;
+    size_t nb = 0;
+    astg_status s = guard(h, [&] { nb = h->getArray(name, dst, bytes); });
+    if (bytes_needed) *bytes_needed = nb;
+    if (s == ASTG_OK && !dst) return ASTG_BAD_ARG;
+    return s;
+}
+
+astg_status astg_set(astg_handle* h, const char* name, const void* src, size_t bytes) {
+    if (!h || !name || !src) return ASTG_BAD_ARG;
+    return guard(h, [&] { h->setArray(name, src, bytes); });
+}
+
+astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32_t* col, const double* val,
+                       const double* b, double* x, double rel_tol, int max_iter, astg_precision prec,
+                       astg_solve_stats* stats) {
+    (void)h; (void)n; (void)rowptr; (void)col; (void)val; (void)b; (void)x; (void)rel_tol; (void)max_iter;
+    (void)prec; (void)stats;
+    if (h) h->err = "astg_solve: not available in this build";
+    return ASTG_BAD_ARG;
+}
+
+astg_status astg_max_velocity(astg_handle* h, double* out) {
+    if (!h || !out) return ASTG_BAD_ARG;
+    return guard(h, [&] {
+        std::vector<double> mac((size_t)3 * h->S);
+        h->down(h->F[h->cur].mac, mac.data(), mac.size());
+        double m = 0;
+        for (double v : mac) m = std::max(m, v);
+        *out = m;
+    });
+}
+
+}  // extern "C"

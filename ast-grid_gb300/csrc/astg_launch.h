@@ -1,0 +1,77 @@
+// Host-side declarations of the kernel launchers (implemented in astg_step.cu and astg_pcg.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include "astg_device.cuh"
+
+namespace astg {
+
+constexpr int ROW_W = 32;  // padded row width during assembly (rows have at most ~21 entries)
+
+// scalars of the PCG kept on the device
+enum { SC_RESID0 = 0, SC_TOL, SC_RHO, SC_RESID, SC_ALPHA, SC_BETA, SC_COUNT };
+enum { ISC_ITERS = 0, ISC_CONVERGED, ISC_COUNT };
+
+// Projection workspace (device pointers unless noted); sized for S + H rows.
+struct Proj {
+    int* cnt;      // S
+    int* base;     // S
+    int* bsum;     // scan block sums
+    int* n0;       // device scalars
+    int* nDof;
+    int* nnz;
+    int* pO;       // S
+    int* pT;       // S
+    int* rowCnt;   // rows
+    int* rowPtr;   // rows + 1
+    int* padCol;   // rows * ROW_W
+    double* padVal;
+    double* bRaw;  // rows
+    int* col;      // rows * ROW_W (CSR, compacted)
+    double* val;
+    int* diagPos;  // rows
+    int* tpos;     // CSR position of the mirrored entry
+    double* b;     // rows
+    // MIC(0)
+    double* Lv;      // CSR-aligned factor values (upper entries = columns of L)
+    double* invdiag;
+    double* adiag;
+    int* ready;      // rows, epoch flags
+    int* counter;
+    int sweepBlocks;
+    // PCG
+    double* x;
+    double* r;
+    double* s;
+    double* z;
+    double* part;    // chunk partials
+    double* sc;      // SC_COUNT
+    int* isc;        // ISC_COUNT
+    unsigned long long* amax;
+    int* done;
+    int* hostDone;   // pinned host
+};
+
+void launch_source(const Dev& d, const Fields& F, cudaStream_t st);
+void launch_scalar_ghost(const Dev& d, double* oct, double* til, const double* te, const uint32_t* tf, cudaStream_t st);
+void launch_dual_ghost(const Dev& d, const Fields& F, cudaStream_t st);
+void launch_mean_temperature(const Dev& d, const double* hO, double* parts, const int* partOffDev,
+                             const int* partOffHost, double* amb, cudaStream_t st);
+void launch_force(const Dev& d, const Fields& F, const uint8_t* open, const double* amb, double dt, cudaStream_t st);
+void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);
+void launch_dof_numbering(const Dev& d, const uint8_t* open, Proj& P, cudaStream_t st);
+void launch_assemble(const Dev& d, const Fields& F, const uint8_t* open, Proj& P, const int* hoPtr, const int* hoIdx,
+                     double dt, cudaStream_t st);
+void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st);
+int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& epoch, int batch, cudaStream_t st);
+void launch_pressure_update(const Dev& d, const Fields& F, const uint8_t* open, const int* pO, const int* pT,
+                            const double* p, double dt, cudaStream_t st);
+void launch_dual(const Dev& d, const Fields& F, cudaStream_t st);
+void launch_adjust(const Dev& d, const Fields& cur, const Fields& nxt, uint8_t* open, uint8_t* fixedf, double dt,
+                   cudaStream_t st);
+void launch_tilt_e_ghost(const Dev& d, double* te, uint32_t* tf, cudaStream_t st);
+void launch_advect_scalars(const Dev& d, const Fields& cur, const Fields& nxt, const uint8_t* open, double dt,
+                           cudaStream_t st);
+void launch_advect_velocity(const Dev& d, const Fields& cur, const Fields& nxt, double dt, cudaStream_t st);
+void launch_decay(const Dev& d, const Fields& F, cudaStream_t st);
+
+}  // namespace astg

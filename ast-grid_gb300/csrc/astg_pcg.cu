@@ -1,0 +1,769 @@
+// Pressure projection on the GPU: DOF numbering, Laplacian assembly, MIC(0) factorisation and
+// preconditioned CG (FP64 and mixed precision), plus the mean-temperature reduction.
+//
+// Determinism.  Every floating-point reduction uses one fixed tree: chunks of 2048 elements, 256
+// lanes per chunk, lane t adds elements t, t+256, ..., t+1792 of its chunk in order starting from
+// 0.0, the lanes are folded by halving strides (t += t + s for s = 128 ... 1) and the chunk partials
+// are reduced by the same rule.  The CPU oracle implements the same tree, so the FP64 solve is
+// reproducible bit for bit.  Matrix rows are summed sequentially in column order, and the
+// triangular sweeps and the factorisation apply their updates in the reference's order.
+//
+// Dependencies between rows (factorisation, both sweeps) are resolved without global barriers:
+// rows are handed out in dependency order from an atomic counter and each row waits on per-row
+// ready flags of the rows it reads.  Every wait is bounded; on timeout the kernel records
+// DS_WAIT_TIMEOUT in the device status word and carries on, so a wait can never hang the GPU.
+#include "astg_launch.h"
+#include "astg_sample.cuh"
+
+namespace astg {
+
+constexpr int TB = 256;
+static inline int nblk(long long n) { return (int)((n + TB - 1) / TB); }
+constexpr int RED_LANES = 256, RED_PER_LANE = 8, RED_CHUNK = RED_LANES * RED_PER_LANE;
+constexpr long long SPIN_LIMIT = 1LL << 24;  // ~seconds at nanosleep(64): far above any real wait
+
+// ------------------------------------------------------------------ fixed-tree reduction
+__device__ inline double block_tree(double v, double* sh) {
+    int t = threadIdx.x;
+    sh[t] = v;
+    __syncthreads();
+    for (int st = RED_LANES / 2; st >= 1; st >>= 1) {
+        if (t < st) sh[t] = sh[t] + sh[t + st];
+        __syncthreads();
+    }
+    double r = sh[0];
+    __syncthreads();
+    return r;
+}
+// sum of a[i] over [0, n) (chunk partials)
+__global__ void k_tree_sum(const double* a, const long long* nptr, long long nconst, double* part) {
+    __shared__ double sh[RED_LANES];
+    long long n = nptr ? *nptr : nconst;
+    long long base = (long long)blockIdx.x * RED_CHUNK;
+    if (base >= n && blockIdx.x > 0) return;
+    double acc = 0.0;
+    for (int k = 0; k < RED_PER_LANE; ++k) {
+        long long i = base + threadIdx.x + (long long)RED_LANES * k;
+        if (i < n) acc = acc + a[i];
+    }
+    double r = block_tree(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+// sum of a[i] * b[i]
+__global__ void k_tree_dot(const double* a, const double* b, const int* nptr, double* part) {
+    __shared__ double sh[RED_LANES];
+    long long n = *nptr;
+    long long base = (long long)blockIdx.x * RED_CHUNK;
+    if (base >= n && blockIdx.x > 0) return;
+    double acc = 0.0;
+    for (int k = 0; k < RED_PER_LANE; ++k) {
+        long long i = base + threadIdx.x + (long long)RED_LANES * k;
+        if (i < n) acc = acc + a[i] * b[i];
+    }
+    double r = block_tree(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+// one block: folds m <= 2048 chunk partials with the same rule
+__device__ inline double fold_partials(const double* part, long long m, double* sh) {
+    double acc = 0.0;
+    for (int k = 0; k < RED_PER_LANE; ++k) {
+        long long i = threadIdx.x + (long long)RED_LANES * k;
+        if (i < m) acc = acc + part[i];
+    }
+    return block_tree(acc, sh);
+}
+
+// ------------------------------------------------------------------ mean temperature
+// addForce, src/octree_omnigrid_solver3.cpp:922-929: per-level sums of the octagon heat (ghosts
+// included) weighted 1 on level 0 and 8 elsewhere, divided by the weighted count
+__global__ void k_amb(Dev d, const double* parts, const int* partOff, double* amb) {
+    __shared__ double sh[RED_LANES];
+    double total = 0.0;
+    long long count = 0;
+    for (int l = 0; l < d.L; ++l) {
+        long long m = partOff[l + 1] - partOff[l];
+        double s = m > 0 ? fold_partials(parts + partOff[l], m, sh) : 0.0;
+        total += s * (l == 0 ? 1 : 8);
+        count += (long long)(d.lN[l] + d.lG[l]) * (l == 0 ? 1 : 8);
+    }
+    if (threadIdx.x == 0) *amb = total / (double)count;
+}
+void launch_mean_temperature(const Dev& d, const double* hO, double* parts, const int* partOffDev,
+                             const int* partOffHost, double* amb, cudaStream_t st) {
+    for (int l = 0; l < d.L; ++l) {
+        long long n = d.lN[l] + d.lG[l];
+        int m = partOffHost[l + 1] - partOffHost[l];
+        if (m > 0) k_tree_sum<<<m, RED_LANES, 0, st>>>(hO + d.loff[l], nullptr, n, parts + partOffHost[l]);
+    }
+    k_amb<<<1, RED_LANES, 0, st>>>(d, parts, partOffDev, amb);
+}
+
+// ------------------------------------------------------------------ exclusive scan (int)
+constexpr int SCAN_B = 1024;
+__global__ void k_scan_block(const int* in, int* out, int* bsum, long long n) {
+    __shared__ int sh[SCAN_B];
+    long long i = (long long)blockIdx.x * SCAN_B + threadIdx.x;
+    int v = i < n ? in[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < SCAN_B; off <<= 1) {
+        int t = threadIdx.x >= off ? sh[threadIdx.x - off] : 0;
+        __syncthreads();
+        sh[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (i < n) out[i] = sh[threadIdx.x] - v;
+    if (threadIdx.x == SCAN_B - 1) bsum[blockIdx.x] = sh[threadIdx.x];
+}
+__global__ void k_scan_sums(int* bsum, int nb, int* total) {
+    if (threadIdx.x != 0) return;
+    int acc = 0;
+    for (int b = 0; b < nb; ++b) {
+        int v = bsum[b];
+        bsum[b] = acc;
+        acc += v;
+    }
+    *total = acc;
+}
+__global__ void k_scan_add(int* out, const int* bsum, long long n) {
+    long long i = (long long)blockIdx.x * SCAN_B + threadIdx.x;
+    if (i < n) out[i] += bsum[blockIdx.x];
+}
+// out = exclusive scan of in[0..n); *total = sum.  bsum needs ceil(n/1024) ints.
+static void exclusive_scan(const int* in, int* out, int* bsum, int* total, long long n, cudaStream_t st) {
+    int nb = (int)((n + SCAN_B - 1) / SCAN_B);
+    k_scan_block<<<nb, SCAN_B, 0, st>>>(in, out, bsum, n);
+    k_scan_sums<<<1, 32, 0, st>>>(bsum, nb, total);
+    k_scan_add<<<nb, SCAN_B, 0, st>>>(out, bsum, n);
+}
+
+// ------------------------------------------------------------------ DOF numbering
+// updateIndexParallel, src/octree_omnigrid_solver3.cpp:292-347: in slot order, a valid octagon
+// then an open tilt take the next index; ghosts get -1; half tilts are appended in list order;
+// the tilt indices are then propagated to ghosts (OctreeVertexCenteredGrid3<int>::updateGhost,
+// src/octree_vertex_centered_grid3.cpp:47-64)
+__global__ void k_dof_count(Dev d, const uint8_t* open, int* cnt) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.S) return;
+    int c = 0;
+    if (!(slot_f(d, s) & SF_GHOST)) c = (oct_valid(d, slot_l(d, s), slot_x(d, s), slot_y(d, s), slot_z(d, s)) ? 1 : 0) + (open[s] ? 1 : 0);
+    cnt[s] = c;
+}
+__global__ void k_dof_assign(Dev d, const uint8_t* open, const int* base, int* pO, int* pT) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.S) return;
+    if (slot_f(d, s) & SF_GHOST) { pO[s] = -1; pT[s] = -1; return; }
+    bool ov = oct_valid(d, slot_l(d, s), slot_x(d, s), slot_y(d, s), slot_z(d, s));
+    pO[s] = ov ? base[s] : -1;
+    pT[s] = open[s] ? base[s] + (ov ? 1 : 0) : -1;
+}
+__global__ void k_dof_half(Dev d, int* pT, const int* n0, int* nDof) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d.H) pT[d.half[i]] = *n0 + i;
+    if (i == 0) *nDof = *n0 + d.H;
+}
+__global__ void k_dof_ghost(Dev d, int* pT, int l) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.lG[l]) return;
+    int s = d.loff[l] + d.lN[l] + i;
+    int x = slot_x(d, s), y = slot_y(d, s), z = slot_z(d, s);
+    if (slot_f(d, s) & SF_FROM_COARSE) {
+        if ((x & 1) || (y & 1) || (z & 1)) return;
+        pT[s] = pT[req(d, l + 1, x >> 1, y >> 1, z >> 1)];
+    } else {
+        pT[s] = pT[req(d, l - 1, x << 1, y << 1, z << 1)];
+    }
+}
+void launch_dof_numbering(const Dev& d, const uint8_t* open, Proj& P, cudaStream_t st) {
+    k_dof_count<<<nblk(d.S), TB, 0, st>>>(d, open, P.cnt);
+    exclusive_scan(P.cnt, P.base, P.bsum, P.n0, d.S, st);
+    k_dof_assign<<<nblk(d.S), TB, 0, st>>>(d, open, P.base, P.pO, P.pT);
+    k_dof_half<<<nblk(d.H > 0 ? d.H : 1), TB, 0, st>>>(d, P.pT, P.n0, P.nDof);
+    for (int l = 0; l < d.L; ++l)
+        if (d.lG[l]) k_dof_ghost<<<nblk(d.lG[l]), TB, 0, st>>>(d, P.pT, l);
+}
+
+// ------------------------------------------------------------------ assembly
+// project(), src/octree_omnigrid_solver3.cpp:350-653.  Each row is built in registers with the
+// reference's set/add semantics (PCG::SparseMatrix::set_element / add_to_element), sorted by
+// column and written to a padded row buffer of width ROW_W; contributions of half tilts to the
+// coarse octagon rows they face are gathered per octagon in half-tilt list order.
+struct RowBuf {
+    int n;
+    int col[ROW_W];
+    double val[ROW_W];
+    ASTG_HD void set(int c, double v) {
+        for (int k = 0; k < n; ++k)
+            if (col[k] == c) { val[k] = v; return; }
+        if (n < ROW_W) { col[n] = c; val[n] = v; }
+        ++n;
+    }
+    ASTG_HD void add(int c, double v) {
+        for (int k = 0; k < n; ++k)
+            if (col[k] == c) { val[k] += v; return; }
+        if (n < ROW_W) { col[n] = c; val[n] = v; }
+        ++n;
+    }
+};
+__device__ inline void store_row(const Dev& d, const Proj& P, int r, RowBuf& rb, double b) {
+    if (rb.n > ROW_W) { report(d, DS_MISSING_NODE); rb.n = ROW_W; }
+    for (int i = 1; i < rb.n; ++i) {  // insertion sort by column
+        int c = rb.col[i];
+        double v = rb.val[i];
+        int j = i - 1;
+        while (j >= 0 && rb.col[j] > c) { rb.col[j + 1] = rb.col[j]; rb.val[j + 1] = rb.val[j]; --j; }
+        rb.col[j + 1] = c;
+        rb.val[j + 1] = v;
+    }
+    P.rowCnt[r] = rb.n;
+    for (int i = 0; i < rb.n; ++i) {
+        P.padCol[(size_t)r * ROW_W + i] = rb.col[i];
+        P.padVal[(size_t)r * ROW_W + i] = rb.val[i];
+    }
+    P.bRaw[r] = b;
+}
+__global__ void k_asm_oct(Dev d, Fields F, Proj P, const int* hoPtr, const int* hoIdx) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.S || (slot_f(d, s) & SF_GHOST)) return;
+    int ci = P.pO[s];
+    int l = slot_l(d, s), x = slot_x(d, s), y = slot_y(d, s), z = slot_z(d, s);
+    if (ci < 0 || !oct_valid(d, l, x, y, z)) return;
+    double h = d.ldh[l];
+    double center = 0, tb = 0, tC = 0, tK = 0;
+    RowBuf rb;
+    rb.n = 0;
+    for (int i = 0; i < 6; ++i) {
+        int axis = i / 2;
+        int nx = x + OCT_NB[i][0], ny = y + OCT_NB[i][1], nz = z + OCT_NB[i][2];
+        if (oct_valid(d, l, nx, ny, nz) && is_ghost_node(d, l, nx, ny, nz)) continue;
+        double area = h * h;
+        for (int m = 0; m <= 1; ++m)
+            for (int n = 0; n <= 1; ++n) {
+                int t[3] = {x, y, z};
+                t[axis] += (i & 1) ? 0 : 1;
+                t[(axis + 1) % 3] += m;
+                t[(axis + 2) % 3] += n;
+                double e = F.te[req(d, l, t[0], t[1], t[2])];
+                area -= e * e * 0.5;
+            }
+        int fs = req(d, l, x + OCT_NB_FACE[i][0], y + OCT_NB_FACE[i][1], z + OCT_NB_FACE[i][2]);
+        if (oct_valid(d, l, nx, ny, nz)) {
+            double term = d.wMac[(size_t)axis * d.S + fs];
+            int ti = P.pO[req(d, l, nx, ny, nz)];
+            if (ti >= 0) {
+                tC = term * area / h;
+                tK = area * term;
+                rb.set(ti, -tC);
+            } else { tC = 0; tK = 0; }
+        } else if ((d.closedMask >> i) & 1) {
+            tC = 0; tK = 0;
+        } else {
+            tK = area;
+            tC = tK / h;
+        }
+        center += tC;
+        tb += ((i & 1) ? 1 : -1) * tK * F.mac[(size_t)axis * d.S + fs];
+    }
+    for (int i = 0; i < 8; ++i) {
+        int ns = req(d, l, x + OCT_NB_TILT[i][0], y + OCT_NB_TILT[i][1], z + OCT_NB_TILT[i][2]);
+        uint32_t f = F.tf[ns];
+        int re = ((i & 1) ? 8 : 6) - i;
+        if (!(f & TF_CLOSED) || (f & TF_HALF)) {
+            double e = F.te[ns];
+            double area = e * e * SQRT3 * 0.5;
+            double term = d.wTilt[(size_t)ns * 8 + re];
+            int ti = P.pT[ns];
+            if (ti >= 0) {
+                tC = term * area / (h * SQRT3 * 0.5);
+                tK = area * term;
+                rb.add(ti, -tC);
+            } else { tC = 0; tK = 0; }
+            center += tC;
+            tb += (i < 4 ? -1 : 1) * tK * F.tv[(size_t)ns * 8 + re];
+        }
+    }
+    if (fabs(center) < EPS) { center = 1; tb = 0; }
+    rb.set(ci, center);
+    // half tilts facing this octagon (src/octree_omnigrid_solver3.cpp:572-581)
+    for (int q = hoPtr[s]; q < hoPtr[s + 1]; ++q) {
+        int hs = d.half[hoIdx[q]];
+        int hci = P.pT[hs];
+        if (hci < 0) continue;
+        int dir = tf_dir(F.tf[hs]);
+        int oi = HALF_SLOT[dir][4];
+        double e = F.te[hs];
+        double area = e * e * 2;
+        double hh = d.ldh[slot_l(d, hs)];
+        double tw = d.wTilt[(size_t)hs * 8 + oi];
+        double u = F.tv[(size_t)hs * 8 + oi];
+        rb.add(ci, tw * area / hh);
+        rb.add(hci, -tw * area / hh);
+        tb += (dir < 3 ? -1 : 1) * u * tw * area;
+    }
+    store_row(d, P, ci, rb, tb);
+}
+__global__ void k_asm_tilt(Dev d, Fields F, Proj P, const uint8_t* open) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.S || (slot_f(d, s) & SF_GHOST)) return;
+    int ci = P.pT[s];
+    if (!open[s] || ci < 0) return;
+    int l = slot_l(d, s), x = slot_x(d, s), y = slot_y(d, s), z = slot_z(d, s);
+    double e = F.te[s];
+    double center = 0, tb = 0, tC = 0, tK = 0;
+    const double* u = F.tv + (size_t)s * 8;
+    const double* tw = d.wTilt + (size_t)s * 8;
+    double area = e * e * SQRT3 * 0.5;
+    RowBuf rb;
+    rb.n = 0;
+    for (int i = 0; i < 8; ++i) {
+        NbOct nb = tilt_nb_oct(d, l, x, y, z, i);
+        if (!nb.some) {
+            if (!oct_valid(d, l, x + TILT_NB_OCT[i][0], y + TILT_NB_OCT[i][1], z + TILT_NB_OCT[i][2])) {
+                tC = area / (d.ldh[l] * SQRT3 / 3.0);
+                tK = area;
+                center += tC;
+                tb += (i < 4 ? -1 : 1) * tK * u[i];
+            }
+            continue;
+        }
+        if (oct_valid(d, nb.l, nb.x, nb.y, nb.z)) {
+            double h2 = d.ldh[nb.l];
+            int ti = P.pO[req(d, nb.l, nb.x, nb.y, nb.z)];
+            if (ti >= 0) {
+                tC = tw[i] * area / (h2 * SQRT3 * 0.5);
+                tK = area * tw[i];
+                rb.set(ti, -tC);
+            } else { tC = 0; tK = 0; }
+        } else {
+            tC = area / (d.ldh[l] * SQRT3 / 3.0);
+            tK = area;
+        }
+        center += tC;
+        tb += (i < 4 ? -1 : 1) * tK * u[i];
+    }
+    if (fabs(center) < EPS) center = 1;
+    rb.set(ci, center);
+    store_row(d, P, ci, rb, tb);
+}
+__global__ void k_asm_half(Dev d, Fields F, Proj P) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.H) return;
+    int hs = d.half[i];
+    int ci = P.pT[hs];
+    if (ci < 0) return;
+    int l = slot_l(d, hs), x = slot_x(d, hs), y = slot_y(d, hs), z = slot_z(d, hs);
+    int dir = tf_dir(F.tf[hs]);
+    double e = F.te[hs];
+    double area = e * e * 2;
+    double h = d.ldh[l];
+    double center = 0, tb = 0, tC = 0, tK = 0;
+    const double* u = F.tv + (size_t)hs * 8;
+    const double* tw = d.wTilt + (size_t)hs * 8;
+    int id[3] = {x >> 1, y >> 1, z >> 1};
+    id[dir % 3] -= dir < 3 ? 1 : 0;
+    int oi = HALF_SLOT[dir][4];
+    RowBuf rb;
+    rb.n = 0;
+    if (l + 1 < d.L && oct_valid(d, l + 1, id[0], id[1], id[2])) {
+        int ti = P.pO[req(d, l + 1, id[0], id[1], id[2])];
+        if (ti >= 0) {
+            center += tw[oi] * area / h;
+            rb.add(ti, -tw[oi] * area / h);
+            tb += (dir < 3 ? 1 : -1) * u[oi] * tw[oi] * area;
+        }
+    } else {
+        int axis = (dir % 3) * 2 + (dir >= 3);
+        if ((d.closedMask >> axis) & 1) { tC = 0; tK = area; }
+        else { tC = 1000; tK = area; }
+        center += tC;
+        tb += (dir < 3 ? 1 : -1) * u[oi] * area;
+    }
+    area = e * e * SQRT3 * 0.5;
+    for (int k = 0; k < 8; ++k) {
+        if (!half_listed(dir, k)) continue;
+        int nx = x + TILT_NB_OCT[k][0], ny = y + TILT_NB_OCT[k][1], nz = z + TILT_NB_OCT[k][2];
+        if (oct_valid(d, l, nx, ny, nz)) {
+            int ti = P.pO[req(d, l, nx, ny, nz)];
+            if (ti >= 0) {
+                tC = area * tw[k] / (h * SQRT3 * 0.5);
+                tK = area * tw[k];
+                rb.set(ti, -tC);
+            } else { tC = 0; tK = 0; }
+        } else {
+            report(d, DS_MISSING_NODE);  // the reference throws here (:641)
+            tC = 0; tK = 0;
+        }
+        center += tC;
+        tb += (k < 4 ? -1 : 1) * tK * u[k];
+    }
+    rb.add(ci, center);
+    store_row(d, P, ci, rb, tb);
+}
+// rows -> CSR, b scaled by rho/dt (BLAS::scale, :651), diagonal positions
+__global__ void k_csr_fill(Proj P, double scale) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= *P.nDof) return;
+    int o = P.rowPtr[r], n = P.rowCnt[r];
+    int dg = -1;
+    for (int i = 0; i < n; ++i) {
+        int c = P.padCol[(size_t)r * ROW_W + i];
+        P.col[o + i] = c;
+        P.val[o + i] = P.padVal[(size_t)r * ROW_W + i];
+        if (c == r) dg = o + i;
+    }
+    P.diagPos[r] = dg;
+    P.b[r] = P.bRaw[r] * scale;
+}
+__global__ void k_rowptr_last(Proj P) {
+    int n = *P.nDof;
+    P.rowPtr[n] = *P.nnz;
+}
+// position of the mirrored entry (c, r) for every off-diagonal entry (r, c); the pattern is
+// symmetric (the reference asserts it, :654), a missing mirror is reported
+__global__ void k_transpose_map(const Dev d, Proj P) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= *P.nDof) return;
+    for (int q = P.rowPtr[r]; q < P.rowPtr[r + 1]; ++q) {
+        int c = P.col[q];
+        int t = -1;
+        if (c != r) {
+            int lo = P.rowPtr[c], hi = P.rowPtr[c + 1] - 1;
+            while (lo <= hi) {
+                int mid = (lo + hi) >> 1;
+                int v = P.col[mid];
+                if (v == r) { t = mid; break; }
+                if (v < r) lo = mid + 1; else hi = mid - 1;
+            }
+            if (t < 0) report(d, DS_MISSING_NODE);
+        }
+        P.tpos[q] = t;
+    }
+}
+__global__ void k_zero_rows(Proj P, int maxRows) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < maxRows) { P.rowCnt[r] = 0; P.bRaw[r] = 0; }
+}
+void launch_assemble(const Dev& d, const Fields& F, const uint8_t* open, Proj& P, const int* hoPtr, const int* hoIdx,
+                     double dt, cudaStream_t st) {
+    int maxRows = d.S + d.H;
+    k_zero_rows<<<nblk(maxRows), TB, 0, st>>>(P, maxRows);
+    k_asm_oct<<<nblk(d.S), TB, 0, st>>>(d, F, P, hoPtr, hoIdx);
+    k_asm_tilt<<<nblk(d.S), TB, 0, st>>>(d, F, P, open);
+    if (d.H) k_asm_half<<<nblk(d.H), TB, 0, st>>>(d, F, P);
+    exclusive_scan(P.rowCnt, P.rowPtr, P.bsum, P.nnz, maxRows, st);
+    k_rowptr_last<<<1, 1, 0, st>>>(P);
+    k_csr_fill<<<nblk(maxRows), TB, 0, st>>>(P, d.rho / dt);
+    k_transpose_map<<<nblk(maxRows), TB, 0, st>>>(d, P);
+}
+
+// ------------------------------------------------------------------ sync-free helpers
+__device__ inline int ld_flag(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ inline void st_flag(int* p, int v) { asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory"); }
+__device__ inline bool wait_flag(const Dev& d, const int* flag, int epoch) {
+    long long n = 0;
+    while (ld_flag(flag) != epoch) {
+        if (++n > SPIN_LIMIT) {
+            report(d, DS_WAIT_TIMEOUT);
+            return false;
+        }
+        __nanosleep(32);
+    }
+    return true;
+}
+// next row handed out in dependency order (ascending, or descending when rev)
+__device__ inline int grab_row(int* counter) { return atomicAdd(counter, 1); }
+
+// ------------------------------------------------------------------ MIC(0) factorisation
+// factor_modified_incomplete_cholesky0, include/pcgsolver/pcg_solver.h:89-190, in left-looking
+// form: column j applies, for every k < j with L(j,k) != 0 in increasing k, exactly the update
+// the reference's step k applies to column j, then finalises itself.  Column k of L is the upper
+// part of row k of A (same positions in the CSR arrays); Lv holds its values.
+__global__ void k_mic_init(Proj P) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= *P.nDof) return;
+    int dg = P.diagPos[r];
+    double a = dg >= 0 ? P.val[dg] : 0.0;
+    P.invdiag[r] = a;
+    P.adiag[r] = a;
+    for (int q = P.rowPtr[r]; q < P.rowPtr[r + 1]; ++q) P.Lv[q] = P.val[q];
+}
+__global__ void k_mic_factor(Dev d, Proj P, double omega, double minDiag, int epoch) {
+    int n = *P.nDof;
+    for (;;) {
+        int j = grab_row(P.counter);
+        if (j >= n) return;
+        int rj0 = P.rowPtr[j], rj1 = P.rowPtr[j + 1];
+        int dgj = P.diagPos[j];
+        int upj = dgj >= 0 ? dgj + 1 : rj1;  // first entry of column j of L
+        double invd = P.invdiag[j];
+        for (int qq = rj0; qq < rj1; ++qq) {
+            int k = P.col[qq];
+            if (k >= j) break;
+            wait_flag(d, P.ready + k, epoch);
+            if (P.adiag[k] == 0) continue;
+            int tq = P.tpos[qq];  // entry (k, j): L(j, k)
+            double mult = P.Lv[tq];
+            double missing = 0;
+            int a = P.diagPos[k] + 1, ak = P.rowPtr[k + 1];
+            int b = rj0;
+            while (a < ak && P.col[a] < j) {
+                while (b < rj1) {
+                    if (P.col[b] < P.col[a]) ++b;
+                    else if (P.col[b] == P.col[a]) break;
+                    else { missing += P.Lv[a]; break; }
+                }
+                ++a;
+            }
+            if (a < ak && P.col[a] == j) invd -= mult * P.Lv[a];
+            ++a;
+            int bb = upj;
+            while (a < ak && bb < rj1) {
+                if (P.col[bb] < P.col[a]) ++bb;
+                else if (P.col[bb] == P.col[a]) { P.Lv[bb] -= mult * P.Lv[a]; ++a; ++bb; }
+                else { missing += P.Lv[a]; ++a; }
+            }
+            while (a < ak) { missing += P.Lv[a]; ++a; }
+            invd -= omega * mult * missing;
+        }
+        double ad = P.adiag[j];
+        if (ad != 0) {
+            if (invd < minDiag * ad) invd = 1 / sqrt(ad);
+            else invd = 1 / sqrt(invd);
+            for (int q = upj; q < rj1; ++q) P.Lv[q] *= invd;
+        }
+        P.invdiag[j] = invd;
+        __threadfence();
+        st_flag(P.ready + j, epoch);
+    }
+}
+
+// ------------------------------------------------------------------ triangular sweeps (FP64)
+// solve_lower (:196-208) row-oriented and solve_lower_transpose_in_place (:226-238); same
+// per-row operation order as the reference's column-oriented loops
+__global__ void k_sweep_fwd(Dev d, Proj P, const double* r, double* z, int epoch) {
+    if (*P.done) return;
+    int n = *P.nDof;
+    for (;;) {
+        int i = grab_row(P.counter);
+        if (i >= n) return;
+        double acc = r[i];
+        int q0 = P.rowPtr[i], dg = P.diagPos[i];
+        int qend = dg >= 0 ? dg : P.rowPtr[i + 1];
+        for (int q = q0; q < qend; ++q) {
+            int k = P.col[q];
+            if (k >= i) break;
+            wait_flag(d, P.ready + k, epoch);
+            acc = acc - P.Lv[P.tpos[q]] * z[k];
+        }
+        z[i] = acc * P.invdiag[i];
+        __threadfence();
+        st_flag(P.ready + i, epoch);
+    }
+}
+__global__ void k_sweep_bwd(Dev d, Proj P, double* z, int epoch) {
+    if (*P.done) return;
+    int n = *P.nDof;
+    for (;;) {
+        int g = grab_row(P.counter);
+        if (g >= n) return;
+        int i = n - 1 - g;
+        double acc = z[i];
+        int dg = P.diagPos[i];
+        int q0 = dg >= 0 ? dg + 1 : P.rowPtr[i];
+        for (int q = q0; q < P.rowPtr[i + 1]; ++q) {
+            int c = P.col[q];
+            if (c <= i) continue;
+            wait_flag(d, P.ready + c, epoch);
+            acc = acc - P.Lv[q] * z[c];
+        }
+        z[i] = acc * P.invdiag[i];
+        __threadfence();
+        st_flag(P.ready + i, epoch);
+    }
+}
+
+// ------------------------------------------------------------------ PCG (FP64)
+// PCGSolver::solve(VectorXd), include/pcgsolver/pcg_solver.h:366-426
+__global__ void k_copy(const double* a, double* b, const int* nptr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *nptr) b[i] = a[i];
+}
+__global__ void k_zero_vec(double* a, const int* nptr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *nptr) a[i] = 0;
+}
+// max |a| over [0, n): non-negative doubles order like their bit patterns
+__global__ void k_absmax(const double* a, const int* nptr, unsigned long long* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0;
+    if (i < *nptr) v = fabs(a[i]);
+    for (int o = 16; o > 0; o >>= 1) {
+        double w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
+}
+__global__ void k_pcg_start(Proj P, const double* partRho, double tolFactor) {
+    __shared__ double sh[RED_LANES];
+    int n = *P.nDof;
+    long long m = (n + RED_CHUNK - 1) / RED_CHUNK;
+    double rho = fold_partials(partRho, m, sh);
+    if (threadIdx.x == 0) {
+        double r0 = __longlong_as_double((long long)*P.amax);
+        P.sc[SC_RESID0] = r0;
+        P.sc[SC_TOL] = tolFactor * r0;
+        P.sc[SC_RHO] = rho;
+        P.sc[SC_RESID] = r0;
+        if (r0 == 0) { *P.done = 1; P.isc[ISC_ITERS] = 0; P.isc[ISC_CONVERGED] = 1; }
+        else if (rho == 0 || rho != rho) { *P.done = 1; P.isc[ISC_ITERS] = 0; P.isc[ISC_CONVERGED] = 0; }
+        else { *P.done = 0; P.isc[ISC_ITERS] = 0; P.isc[ISC_CONVERGED] = 0; }
+        *P.amax = 0;
+    }
+}
+// z = A s, partial dots of s . z (lane layout of the fixed tree: thread t owns rows t + 256 k)
+__global__ void k_spmv_dot(Proj P, const double* s, double* z, double* part) {
+    __shared__ double sh[RED_LANES];
+    if (*P.done) return;
+    int n = *P.nDof;
+    long long base = (long long)blockIdx.x * RED_CHUNK;
+    if (base >= n) return;
+    double acc = 0.0;
+    for (int k = 0; k < RED_PER_LANE; ++k) {
+        long long i = base + threadIdx.x + (long long)RED_LANES * k;
+        if (i < n) {
+            double t = 0;
+            for (int q = P.rowPtr[i]; q < P.rowPtr[i + 1]; ++q) t += P.val[q] * s[P.col[q]];
+            z[i] = t;
+            acc = acc + s[i] * t;
+        }
+    }
+    double r = block_tree(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+__global__ void k_alpha(Proj P, const double* part) {
+    __shared__ double sh[RED_LANES];
+    if (*P.done) return;
+    int n = *P.nDof;
+    long long m = (n + RED_CHUNK - 1) / RED_CHUNK;
+    double dsz = fold_partials(part, m, sh);
+    if (threadIdx.x == 0) P.sc[SC_ALPHA] = P.sc[SC_RHO] / dsz;
+}
+__global__ void k_update_xr(Proj P, double* x, double* r, const double* s, const double* z) {
+    if (*P.done) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = *P.nDof;
+    double alpha = P.sc[SC_ALPHA];
+    double v = 0;
+    if (i < n) {
+        x[i] += alpha * s[i];
+        double ri = r[i] + -alpha * z[i];
+        r[i] = ri;
+        v = fabs(ri);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        double w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(P.amax, (unsigned long long)__double_as_longlong(v));
+}
+__global__ void k_check(Proj P, int maxIter) {
+    if (*P.done) return;
+    double res = __longlong_as_double((long long)*P.amax);
+    *P.amax = 0;
+    int it = P.isc[ISC_ITERS];
+    P.sc[SC_RESID] = res;
+    if (res <= P.sc[SC_TOL]) {
+        P.isc[ISC_ITERS] = it + 1;
+        P.isc[ISC_CONVERGED] = 1;
+        *P.done = 1;
+    } else if (it + 1 >= maxIter) {
+        P.isc[ISC_ITERS] = it + 1;
+        P.isc[ISC_CONVERGED] = 0;
+        *P.done = 1;
+    } else {
+        P.isc[ISC_ITERS] = it + 1;
+    }
+}
+__global__ void k_beta(Proj P, const double* part) {
+    __shared__ double sh[RED_LANES];
+    if (*P.done) return;
+    int n = *P.nDof;
+    long long m = (n + RED_CHUNK - 1) / RED_CHUNK;
+    double rn = fold_partials(part, m, sh);
+    if (threadIdx.x == 0) {
+        P.sc[SC_BETA] = rn / P.sc[SC_RHO];
+        P.sc[SC_RHO] = rn;
+    }
+}
+__global__ void k_update_s(Proj P, double* s, const double* z) {
+    if (*P.done) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *P.nDof) return;
+    s[i] = z[i] + P.sc[SC_BETA] * s[i];
+}
+__global__ void k_reset_counter(int* c) { *c = 0; }
+
+// one preconditioner application z = (L L^T)^-1 r
+static void precond(const Dev& d, Proj& P, const double* r, double* z, int& epoch, int rowsMax, cudaStream_t st) {
+    int warps = P.sweepBlocks;
+    k_reset_counter<<<1, 1, 0, st>>>(P.counter);
+    k_sweep_fwd<<<warps, 128, 0, st>>>(d, P, r, z, ++epoch);
+    k_reset_counter<<<1, 1, 0, st>>>(P.counter);
+    k_sweep_bwd<<<warps, 128, 0, st>>>(d, P, z, ++epoch);
+    (void)rowsMax;
+}
+
+void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st) {
+    int maxRows = d.S + d.H;
+    k_mic_init<<<nblk(maxRows), TB, 0, st>>>(P);
+    k_reset_counter<<<1, 1, 0, st>>>(P.counter);
+    k_mic_factor<<<P.sweepBlocks, 128, 0, st>>>(d, P, omega, minDiag, ++epoch);
+}
+
+// Runs the FP64 PCG to completion.  Iterations are launched in batches; every kernel returns at
+// once when the device "done" flag is set, so a batch that overshoots does no work.
+int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& epoch, int batch, cudaStream_t st) {
+    int maxRows = d.S + d.H;
+    int chunks = (maxRows + RED_CHUNK - 1) / RED_CHUNK;
+    double* x = P.x;
+    double* r = P.r;
+    double* s = P.s;
+    double* z = P.z;
+    k_zero_vec<<<nblk(maxRows), TB, 0, st>>>(x, P.nDof);
+    k_copy<<<nblk(maxRows), TB, 0, st>>>(P.b, r, P.nDof);
+    cudaMemsetAsync(P.amax, 0, sizeof(unsigned long long), st);
+    cudaMemsetAsync(P.done, 0, sizeof(int), st);
+    k_absmax<<<nblk(maxRows), TB, 0, st>>>(r, P.nDof, P.amax);
+    precond(d, P, r, z, epoch, maxRows, st);
+    k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part);
+    k_pcg_start<<<1, RED_LANES, 0, st>>>(P, P.part, tolFactor);
+    k_copy<<<nblk(maxRows), TB, 0, st>>>(z, s, P.nDof);
+    int launched = 0;
+    int hostDone = 0;
+    while (launched < maxIter) {
+        int nb = batch;
+        if (launched + nb > maxIter) nb = maxIter - launched;
+        for (int it = 0; it < nb; ++it) {
+            k_spmv_dot<<<chunks, RED_LANES, 0, st>>>(P, s, z, P.part);
+            k_alpha<<<1, RED_LANES, 0, st>>>(P, P.part);
+            k_update_xr<<<nblk(maxRows), TB, 0, st>>>(P, x, r, s, z);
+            k_check<<<1, 1, 0, st>>>(P, maxIter);
+            precond(d, P, r, z, epoch, maxRows, st);
+            k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part);
+            k_beta<<<1, RED_LANES, 0, st>>>(P, P.part);
+            k_update_s<<<nblk(maxRows), TB, 0, st>>>(P, s, z);
+        }
+        launched += nb;
+        cudaMemcpyAsync(P.hostDone, P.done, sizeof(int), cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        hostDone = *P.hostDone;
+        if (hostDone) break;
+    }
+    return launched;
+}
+
+}  // namespace astg

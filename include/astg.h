@@ -1,0 +1,142 @@
+/*
+ * astg.h -- C ABI of the GB300 octree smoke-step library (libastgrid_gpu.so).
+ *
+ * Drop-in boundary for the AST-modified octree smoke step of YuweiXiao/AST-Grid
+ * (OctreeOmniGridSolver3 / OmniBoundarySolver3 / PCGSolver).  Host callers pass plain pointers
+ * and sizes; all device memory belongs to the handle; every call returns an astg_status and no
+ * C++ exception crosses the boundary.  One CUDA stream per handle; a handle is
+ * thread-compatible, not thread-safe.  Arrays exchanged through astg_get / astg_set are in the
+ * reference's storage order (level-major, then the reference's layout index: non-ghost cells in
+ * raster z-y-x order followed by ghosts in discovery order), so they can be compared with the
+ * reference's own grids element by element.
+ */
+#ifndef ASTG_H
+#define ASTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum astg_status {
+    ASTG_OK = 0,
+    ASTG_BAD_ARG = 1,
+    ASTG_CUDA_ERROR = 2,
+    ASTG_NOT_CONVERGED = 3,
+    ASTG_DEVICE_WAIT_TIMEOUT = 4,
+    ASTG_NAN_DETECTED = 5,
+    ASTG_LAYOUT_ERROR = 6,
+    ASTG_NO_DEVICE = 7
+} astg_status;
+
+typedef enum astg_precision {
+    ASTG_FP64 = 0,  /* all-FP64 PCG, the drop-in form */
+    ASTG_MIXED = 1  /* FP32 SpMV / preconditioner / axpy inside FP64 defect correction */
+} astg_precision;
+
+/* Solver and scene parameters.  Defaults (astg_default_params) are the benchmark scene:
+ * unit cube, walls closed except z+, sphere source r = 0.06 at (0.5, 0.5, 0.12), buoyancy -0.1
+ * (density) and +1.0 (temperature), no decay, rho = 2, MIC(0) omega 0.97 / min diagonal ratio
+ * 0.25, PCG tolerance 1e-6 relative to |b|_inf, at most 3000 iterations. */
+typedef struct astg_params {
+    int coarsest;         /* cells per axis on the coarsest level */
+    int levels;           /* numOctreeLayer: level 0 is the finest, res = coarsest << (levels-1) */
+    double tol;           /* PCG tolerance factor (set_solver_parameters) */
+    int max_iter;
+    double omega;         /* MIC(0) modification parameter */
+    double min_diag;      /* MIC(0) minimum diagonal ratio */
+    double rho;           /* fluid density (setRho) */
+    double buoy_density;  /* _buoyancySmokeDensityFactor */
+    double buoy_temp;     /* _buoyancyTemperatureFactor */
+    double decay;         /* _smokeDecayFactor and _temperatureDecayFactor */
+    int closed_mask;      /* walls closed: bit 0 x+, 1 x-, 2 y+, 3 y-, 4 z+, 5 z- */
+    int tilt_adaptivity;  /* enableTiltAdaptivity */
+    double src_x, src_y, src_z, src_r;  /* sphere source re-injected every step (r <= 0: none) */
+    double noise;         /* amplitude of the initial divergence-free curl noise */
+    uint64_t seed;        /* seed of the curl noise */
+    int precision;        /* astg_precision of astg_step's projection */
+    int device;           /* CUDA device ordinal */
+} astg_params;
+
+typedef struct astg_handle astg_handle;
+
+typedef struct astg_solve_stats {
+    int iterations;       /* PCG iterations (inner iterations for ASTG_MIXED) */
+    int outer;            /* defect-correction cycles (ASTG_MIXED), 0 for FP64 */
+    int converged;
+    int n;                /* system size */
+    long long nnz;
+    double residual;      /* final |r|_inf */
+    double tolerance;     /* tol * |b|_inf */
+    double ms;            /* device time of the solve (CUDA events) */
+} astg_solve_stats;
+
+typedef struct astg_step_stats {
+    astg_solve_stats solve;
+    double ms_total;      /* device time of the whole step */
+    double ms_force, ms_project, ms_advect;
+} astg_step_stats;
+
+/* Fills p with the benchmark defaults for a given coarsest resolution and level count. */
+void astg_default_params(astg_params* p, int coarsest, int levels);
+
+/* OctreeOmniGridSolver3(res, spac, name) + initialize() (src/octree_omnigrid_solver3.cpp:45-149):
+ * builds the octree from split_map (res^3 level ids, index (z*res + y)*res + x; NULL = the
+ * benchmark scene's refinement around the source), constrains the tilted cells, sets the cut-cell
+ * weights, uploads everything and initialises the velocity with the curl noise. */
+astg_status astg_create(const astg_params* p, const int32_t* split_map, astg_handle** out);
+void astg_destroy(astg_handle* h);
+const char* astg_last_error(const astg_handle* h);
+
+/* Solver::update(dt) with useFixedTimeStep (src/solver.cpp:8-46) ->
+ * OctreeOmniGridSolver3::onUpdate (src/octree_omnigrid_solver3.cpp:222-249). */
+astg_status astg_step(astg_handle* h, double dt, astg_step_stats* stats);
+
+/* One stage of onUpdate: 0 scene setup (source), 1 addForce, 2 wall constraint + velocity ghosts,
+ * 3 project (:350-679), 4 constraint + ghosts + dual grid, 5 advect (:850-914). */
+astg_status astg_stage(astg_handle* h, int stage, double dt);
+
+/* PCGSolver::set_solver_parameters (include/pcgsolver/pcg_solver.h:267-274). */
+astg_status astg_set_solver_parameters(astg_handle* h, double tol, int max_iter, double omega, double min_diag);
+astg_status astg_set_precision(astg_handle* h, astg_precision prec);
+
+/* Statistics of the last projection. */
+astg_status astg_last_solve(const astg_handle* h, astg_solve_stats* out);
+
+/* Sizes: 0 slots, 1 levels, 2 finest resolution, 3 DOFs of the last projection,
+ * 4 half tilts, 5 non-zeros of the last matrix. */
+long long astg_size(const astg_handle* h, int what);
+
+/* Copy a state array out of / into the handle.  Names (element type):
+ *   density_oct density_tilt heat_oct heat_tilt tilt_e (f64, slots)  mac (f64, 3 x slots)
+ *   tilt_vel (f64, slots x 8)  dual_oct dual_tilt (f64, slots x 3)
+ *   tilt_flags (i32, slots x 2: bit 0 largest, 1 closed, 2 fixed, 3 T-joint, 4 closed by T-joint,
+ *   5 half tilt; half direction)  tilt_open (u8, slots: bit 0 open, bit 1 fixed)
+ *   prefix "t_" = the swap-partner buffer of the reference's double-buffered grids;
+ * read only: slot_coords (i32, slots x 4: x y z flags) level_sizes (i32, levels x 3)
+ *   half_tilts t_joints closed_by_half_tilt (i64 packed level coordinates) split_map (i32)
+ *   w_mac w_tilt dual_tables (f64) pindex_oct pindex_tilt (i32) A_rowptr A_col (i32) A_val b p
+ *   (f64) pcg_iters (i32 x 2) ambT (f64).
+ * bytes must equal the array's size (astg_get with dst = NULL returns ASTG_BAD_ARG and stores
+ * the size in *bytes_needed when that pointer is not NULL). */
+astg_status astg_get(astg_handle* h, const char* name, void* dst, size_t bytes, size_t* bytes_needed);
+astg_status astg_set(astg_handle* h, const char* name, const void* src, size_t bytes);
+
+/* Stand-alone PCGSolver::solve(A, b, x) on a CSR matrix held in host memory
+ * (include/pcgsolver/pcg_solver.h:366-426): MIC(0) preconditioner, stop when
+ * |r|_inf <= rel_tol * |b|_inf.  Rows must be sorted by column and the pattern symmetric. */
+astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32_t* col, const double* val,
+                       const double* b, double* x, double rel_tol, int max_iter, astg_precision prec,
+                       astg_solve_stats* stats);
+
+/* Maximum |MAC velocity| over all faces, the quantity OctreeOmniGridSolver3::cfl divides by
+ * the finest spacing (src/octree_omnigrid_solver3.cpp:1066-1122). */
+astg_status astg_max_velocity(astg_handle* h, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ASTG_H */

@@ -116,7 +116,9 @@ class Oracle:
         return out
 
     def set(self, name, arr):
-        base = name[2:] if name.startswith("t_") else name
+        fields = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct",
+                  "dual_tilt", "tilt_e", "tilt_flags", "tilt_open"}
+        base = name[2:] if name.startswith("t_") and name[2:] in fields else name
         dt = np.int32 if base == "tilt_flags" else np.uint8 if base == "tilt_open" else np.float64
         a = np.ascontiguousarray(arr, dtype=dt).ravel()
         rc = lib().orc_set(self._h, name.encode(), a.ctypes.data, a.size)

@@ -2046,10 +2046,15 @@ int orc_set(void* h, const char* name, const void* buf, long long count) {
     auto* s = (oracle::Solver*)h;
     std::string n = name;
     int c = s->cur;
-    if (n.compare(0, 2, "t_") == 0) {
-        c = 1 - c;
-        n = n.substr(2);
-    }
+    static const char* fields[] = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel",
+                                   "dual_oct", "dual_tilt", "tilt_e", "tilt_flags", "tilt_open"};
+    if (n.compare(0, 2, "t_") == 0)
+        for (const char* f : fields)
+            if (n.compare(2, std::string::npos, f) == 0) {
+                c = 1 - c;
+                n = n.substr(2);
+                break;
+            }
     auto ind = [&](std::vector<double>& v) {
         if ((long long)v.size() != count) return 1;
         memcpy(v.data(), buf, sizeof(double) * count);

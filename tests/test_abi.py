@@ -1,0 +1,63 @@
+"""CPU checks of the drop-in boundary: the CUDA library builds, loads and exports every entry
+point include/astg.h declares; the Python front end refuses to run without it."""
+import os
+import re
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "ast-grid_gb300")
+if PKG not in sys.path:
+    sys.path.insert(0, PKG)
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "astg.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(astg_[a-z_0-9]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    import ctypes
+
+    import build_lib
+
+    path = build_lib.build()
+    so = ctypes.CDLL(path)
+    syms = declared_symbols()
+    assert len(syms) >= 10
+    missing = [s for s in syms if not hasattr(so, s)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_python_front_end_lists_the_abi():
+    import ast_solver
+
+    assert sorted(ast_solver.SYMBOLS) == declared_symbols()
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    import ast_solver
+
+    saved = ast_solver._lib
+    ast_solver._lib = None
+    try:
+        with pytest.raises(OSError):
+            ast_solver.lib(str(tmp_path / "nope.so"))
+    finally:
+        ast_solver._lib = saved
+
+
+def test_default_params_match_the_benchmark_scene():
+    import ctypes
+
+    import ast_solver
+
+    p = ast_solver.Params()
+    ast_solver.lib().astg_default_params(ctypes.byref(p), 32, 3)
+    assert (p.coarsest, p.levels, p.max_iter) == (32, 3, 3000)
+    assert (p.tol, p.omega, p.min_diag, p.rho) == (1e-6, 0.97, 0.25, 2.0)
+    assert (p.buoy_density, p.buoy_temp, p.decay) == (-0.1, 1.0, 1.0)
+    assert (p.src_x, p.src_y, p.src_z, p.src_r) == (0.5, 0.5, 0.12, 0.06)
+    assert p.closed_mask == 0b101111  # z+ open
