@@ -21,7 +21,7 @@ FP64, MIXED = 0, 1
 
 # exported symbols of include/astg.h
 SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_stage",
-           "astg_set_solver_parameters", "astg_set_precision", "astg_last_solve", "astg_size", "astg_get", "astg_set",
+           "astg_set_solver_parameters", "astg_set_precision", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
            "astg_solve", "astg_max_velocity"]
 
 
@@ -73,6 +73,7 @@ def lib(path=None):
         L.astg_stage.argtypes = [c_p, ctypes.c_int, ctypes.c_double]
         L.astg_set_solver_parameters.argtypes = [c_p, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.astg_set_precision.argtypes = [c_p, ctypes.c_int]
+        L.astg_set_profiling.argtypes = [c_p, ctypes.c_int]
         L.astg_last_solve.argtypes = [c_p, ctypes.POINTER(SolveStats)]
         L.astg_size.argtypes = [c_p, ctypes.c_int]
         L.astg_size.restype = ctypes.c_longlong
@@ -85,7 +86,7 @@ def lib(path=None):
     return _lib
 
 
-_F64 = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
+_F64 = {"kernel_ms", "density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
         "tilt_e", "w_mac", "w_tilt", "dual_tables", "A_val", "b", "p", "ambT"}
 _I64 = {"half_tilts", "t_joints", "closed_by_half_tilt"}
 _U8 = {"tilt_open"}
@@ -175,6 +176,19 @@ class OctreeSmoke3:
     def set_precision(self, prec):
         self._check(lib().astg_set_precision(self._h, {"fp64": FP64, "mixed": MIXED}.get(prec, prec)))
 
+    def set_profiling(self, on):
+        self._check(lib().astg_set_profiling(self._h, 1 if on else 0))
+
+    def kernel_ms(self):
+        """{kernel: (total ms, launches)} of the profiled PCG kernels."""
+        v = self.get("kernel_ms")
+        names = ["sweep_fwd", "sweep_bwd", "spmv_dot", "mic_factor"]
+        return {n: (float(v[2 * i]), int(v[2 * i + 1])) for i, n in enumerate(names)}
+
+    @property
+    def launches(self):
+        return self.size(6)
+
     def last_solve(self):
         s = SolveStats()
         self._check(lib().astg_last_solve(self._h, ctypes.byref(s)))
@@ -213,6 +227,20 @@ class OctreeSmoke3:
 
     def getHeat(self):
         return self.get("heat_oct")
+
+    def solve(self, rowptr, col, val, b, rel_tol=1e-6, max_iter=3000, precision="fp64"):
+        """PCGSolver::solve(A, b, x) on a CSR system in host memory; returns (x, SolveStats)."""
+        rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+        c = np.ascontiguousarray(col, dtype=np.int32)
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(len(bb))
+        st = SolveStats()
+        prec = {"fp64": FP64, "mixed": MIXED}.get(precision, precision)
+        self._check(lib().astg_solve(self._h, len(bb), rp.ctypes.data, c.ctypes.data, v.ctypes.data, bb.ctypes.data,
+                                     x.ctypes.data, rel_tol, max_iter, prec, ctypes.byref(st)),
+                    allow=(ASTG_NOT_CONVERGED,))
+        return x, st
 
     def max_velocity(self):
         v = ctypes.c_double()

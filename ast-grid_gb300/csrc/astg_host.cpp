@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -92,6 +93,7 @@ struct astg_handle {
     int epoch = 0;
     bool firstSource = true;
     astg_solve_stats last{};
+    KProf prof;
     std::vector<void*> allocs;
 
     template <class T>
@@ -591,7 +593,7 @@ struct astg_handle {
         J.bsum = dalloc<int>((rows + 1023) / 1024 + 1);
         J.n0 = dalloc<int>(1);
         J.nDof = dalloc<int>(1);
-        J.nnz = dalloc<int>(1);
+        J.nnz = dalloc<int>(4);  // nnz, then scan totals of the level schedule
         J.pO = dalloc<int>(S);
         J.pT = dalloc<int>(S);
         J.rowCnt = dalloc<int>(rows);
@@ -609,6 +611,37 @@ struct astg_handle {
         J.adiag = dalloc<double>(rows);
         J.ready = dalloc<int>(rows);
         J.counter = dalloc<int>(1);
+        J.level = dalloc<int>(rows);
+        J.levelCnt = dalloc<int>(rows + 1);
+        J.levelPtr = dalloc<int>(rows + 2);
+        J.nLevels = dalloc<int>(1);
+        J.fill = dalloc<int>(rows + 1);
+        J.perm = dalloc<int>(rows);
+        J.cntF = dalloc<int>(rows);
+        J.cntB = dalloc<int>(rows);
+        J.fptr = dalloc<int>(rows + 1);
+        J.bptr = dalloc<int>(rows + 1);
+        J.fcol = dalloc<int>(rows * ROW_W / 2 + 1);
+        J.fval = dalloc<double>(rows * ROW_W / 2 + 1);
+        J.bcol = dalloc<int>(rows * ROW_W / 2 + 1);
+        J.bval = dalloc<double>(rows * ROW_W / 2 + 1);
+        const char* env = getenv("ASTG_SWEEP");
+        std::string mode = env ? env : "";
+        J.clusterSize = mode == "syncfree" ? 0 : choose_cluster_size(P.device);
+        J.pcCluster = (mode == "syncfree" || mode == "cluster") ? 0 : choose_dsmem_cluster((int)rows, &J.pcSmem);
+        if (J.pcCluster == 0) J.pcSmem = 0;
+        J.rowsCap = (int)rows;
+        if (J.pcCluster) {
+            J.pos = dalloc<int>(rows);
+            J.lcntF = dalloc<int>(rows);
+            J.lcntB = dalloc<int>(rows);
+            J.linvd = dalloc<double>(rows);
+            J.rl = dalloc<double>(rows);
+            J.fcolP = dalloc<int>(rows * PC_MAXE);
+            J.fvalP = dalloc<double>(rows * PC_MAXE);
+            J.bcolP = dalloc<int>(rows * PC_MAXE);
+            J.bvalP = dalloc<double>(rows * PC_MAXE);
+        }
         int sms = 0;
         ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P.device), "attr");
         J.sweepBlocks = std::max(1, sms) * 8;
@@ -638,16 +671,25 @@ struct astg_handle {
         }
     }
 
+    // factorises the system held in the projection workspace and runs the PCG; J.x holds the result
+    void solveCurrent(double tol, int maxIter) {
+        launch_factor(d, J, P.omega, P.min_diag, epoch, st, &prof);
+        if (J.clusterSize > 0 || J.pcCluster > 0) launch_level_schedule(d, J, st);
+        ck(cudaEventRecord(evA, st), "event");
+        launch_pcg_fp64(d, J, tol, maxIter, epoch, 8, st, &prof);
+        ck(cudaEventRecord(evB, st), "event");
+    }
+
     void project(double dt) {
         Fields& C = F[cur];
         launch_dof_numbering(d, dOpen, J, st);
         launch_assemble(d, C, dOpen, J, dHoPtr, dHoIdx, dt, st);
-        launch_factor(d, J, P.omega, P.min_diag, epoch, st);
-        ck(cudaEventRecord(evA, st), "event");
-        launch_pcg_fp64(d, J, P.tol, P.max_iter, epoch, 8, st);
-        ck(cudaEventRecord(evB, st), "event");
+        solveCurrent(P.tol, P.max_iter);
         launch_pressure_update(d, C, dOpen, J.pO, J.pT, J.x, dt, st);
-        // statistics of the solve
+        readSolveStats();
+    }
+
+    void readSolveStats() {
         int isc[ISC_COUNT], n = 0, nnz = 0;
         double sc[SC_COUNT];
         ck(cudaMemcpyAsync(isc, J.isc, sizeof isc, cudaMemcpyDeviceToHost, st), "stats");
@@ -655,6 +697,11 @@ struct astg_handle {
         ck(cudaMemcpyAsync(&n, J.nDof, sizeof n, cudaMemcpyDeviceToHost, st), "stats");
         ck(cudaMemcpyAsync(&nnz, J.nnz, sizeof nnz, cudaMemcpyDeviceToHost, st), "stats");
         ck(cudaStreamSynchronize(st), "project");
+        if (g_cluster_error != cudaSuccess) {
+            cudaError_t e = g_cluster_error;
+            g_cluster_error = cudaSuccess;
+            ck(e, "cluster sweep launch");
+        }
         float ms = 0;
         cudaEventElapsedTime(&ms, evA, evB);
         last.iterations = isc[ISC_ITERS];
@@ -665,6 +712,34 @@ struct astg_handle {
         last.residual = sc[SC_RESID];
         last.tolerance = sc[SC_TOL];
         last.ms = ms;
+    }
+
+    // PCGSolver::solve on a caller-supplied CSR system (uses and overwrites the projection
+    // workspace of the handle)
+    void solveExternal(int n, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
+                       double* x, double tol, int maxIter, astg_solve_stats* stats) {
+        long long rows = (long long)S + H;
+        if (n <= 0 || n > rows) throw std::invalid_argument("astg_solve: n exceeds the handle's capacity (slots + half tilts)");
+        long long nnz = rowptr[n];
+        if (nnz <= 0 || nnz > rows * ROW_W) throw std::invalid_argument("astg_solve: too many non-zeros for the workspace");
+        for (int i = 0; i < n; ++i)
+            if (rowptr[i + 1] - rowptr[i] > ROW_W || rowptr[i + 1] < rowptr[i])
+                throw std::invalid_argument("astg_solve: malformed row pointer or row longer than 32 entries");
+        int nn = n, nz = (int)nnz;
+        ck(cudaMemcpyAsync(J.nDof, &nn, sizeof(int), cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaMemcpyAsync(J.nnz, &nz, sizeof(int), cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaMemcpyAsync(J.rowPtr, rowptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaMemcpyAsync(J.col, col, sizeof(int) * nnz, cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaMemcpyAsync(J.val, val, sizeof(double) * nnz, cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaMemcpyAsync(J.b, b, sizeof(double) * n, cudaMemcpyHostToDevice, st), "upload");
+        launch_external_system(d, J, n, st);
+        checkStatus();
+        solveCurrent(tol, maxIter);
+        readSolveStats();
+        checkStatus();
+        ck(cudaMemcpyAsync(x, J.x, sizeof(double) * n, cudaMemcpyDeviceToHost, st), "download");
+        ck(cudaStreamSynchronize(st), "solve");
+        if (stats) *stats = last;
     }
 
     void stage(int id, double dt) {
@@ -843,6 +918,14 @@ struct astg_handle {
             return nb;
         }
         if (name == "ambT") { size_t nb = need(8); if (dst) down(dAmb, dst, 1); return nb; }
+        if (name == "kernel_ms") {  // f64 x 8: (ms, launches) for fwd sweep, bwd sweep, SpMV+dot, factor
+            size_t nb = need(64);
+            if (dst) {
+                double* o = (double*)dst;
+                for (int k = 0; k < KPROF_KINDS; ++k) { o[2 * k] = prof.ms[k]; o[2 * k + 1] = (double)prof.count[k]; }
+            }
+            return nb;
+        }
         throw std::invalid_argument("astg_get: unknown array " + name0);
     }
 
@@ -979,6 +1062,13 @@ astg_status astg_set_solver_parameters(astg_handle* h, double tol, int max_iter,
     return ASTG_OK;
 }
 
+astg_status astg_set_profiling(astg_handle* h, int on) {
+    if (!h) return ASTG_BAD_ARG;
+    h->prof.on = on != 0;
+    for (int k = 0; k < KPROF_KINDS; ++k) { h->prof.ms[k] = 0; h->prof.count[k] = 0; }
+    return ASTG_OK;
+}
+
 astg_status astg_set_precision(astg_handle* h, astg_precision prec) {
     if (!h || (prec != ASTG_FP64 && prec != ASTG_MIXED)) return ASTG_BAD_ARG;
     h->P.precision = prec;
@@ -1000,6 +1090,8 @@ long long astg_size(const astg_handle* h, int what) {
         case 3: return h->last.n;
         case 4: return h->H;
         case 5: return h->last.nnz;
+        case 6: return astg::g_launches;
+        case 7: return h->J.pcCluster > 0 ? 100 + h->J.pcCluster : h->J.clusterSize;
         default: return -1;
     }
 }
@@ -1021,10 +1113,11 @@ astg_status astg_set(astg_handle* h, const char* name, const void* src, size_t b
 astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32_t* col, const double* val,
                        const double* b, double* x, double rel_tol, int max_iter, astg_precision prec,
                        astg_solve_stats* stats) {
-    (void)h; (void)n; (void)rowptr; (void)col; (void)val; (void)b; (void)x; (void)rel_tol; (void)max_iter;
-    (void)prec; (void)stats;
-    if (h) h->err = "astg_solve: not available in this build";
-    return ASTG_BAD_ARG;
+    if (!h || !rowptr || !col || !val || !b || !x || max_iter <= 0) return ASTG_BAD_ARG;
+    if (prec != ASTG_FP64 && prec != ASTG_MIXED) return ASTG_BAD_ARG;
+    astg_status s = guard(h, [&] { h->solveExternal(n, rowptr, col, val, b, x, rel_tol, max_iter, stats); });
+    if (s == ASTG_OK && !h->last.converged) return ASTG_NOT_CONVERGED;
+    return s;
 }
 
 astg_status astg_max_velocity(astg_handle* h, double* out) {

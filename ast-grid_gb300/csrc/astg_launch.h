@@ -5,7 +5,29 @@
 
 namespace astg {
 
-constexpr int ROW_W = 32;  // padded row width during assembly (rows have at most ~21 entries)
+// number of kernels this library has launched (all handles of the process)
+extern long long g_launches;
+#define ASTG_LAUNCH(...)            \
+    do {                            \
+        ++::astg::g_launches;       \
+        __VA_ARGS__;                \
+    } while (0)
+
+// optional CUDA-event timing of the PCG's kernels: 0 forward sweep, 1 backward sweep,
+// 2 SpMV + dot, 3 MIC(0) factorisation
+constexpr int KPROF_KINDS = 4;
+struct KProf {
+    bool on = false;
+    double ms[KPROF_KINDS] = {0, 0, 0, 0};
+    long long count[KPROF_KINDS] = {0, 0, 0, 0};
+    cudaEvent_t ev[2 * 128];
+    int kind[128];
+    int used = 0;
+    bool created = false;
+};
+
+constexpr int ROW_W = 32;
+constexpr int PC_MAXE = 8;  // factor entries per row held in the padded records  // padded row width during assembly (rows have at most ~21 entries)
 
 // scalars of the PCG kept on the device
 enum { SC_RESID0 = 0, SC_TOL, SC_RHO, SC_RESID, SC_ALPHA, SC_BETA, SC_COUNT };
@@ -38,6 +60,35 @@ struct Proj {
     int* ready;      // rows, epoch flags
     int* counter;
     int sweepBlocks;
+    // level schedule of the lower factor (rows grouped by dependency depth), rebuilt per solve
+    int* level;      // rows: 1 + max level of the rows it depends on
+    int* levelCnt;   // rows + 1
+    int* levelPtr;   // rows + 1
+    int* nLevels;    // device scalar
+    int* fill;       // rows + 1
+    int* perm;       // rows in level order
+    int* cntF;       // rows: lower entries per level-ordered row
+    int* cntB;       // rows: upper entries
+    int* fptr;       // rows + 1
+    int* bptr;
+    int* fcol;       // nnz: level-ordered lower entries (column, factor value)
+    double* fval;
+    int* bcol;       // nnz: level-ordered upper entries
+    double* bval;
+    int clusterSize; // CTAs per cluster of the level-synchronous sweeps (0: sync-free sweeps)
+    int pcCluster;   // CTAs per cluster of the fused DSMEM preconditioner (0: not used)
+    // padded level-ordered records for the fused preconditioner (entry e of row p at e * rowsCap + p)
+    int rowsCap;
+    int* pos;        // rows: level position of each row (inverse of perm)
+    int* lcntF;      // rows: lower entries of the row at level position p
+    int* lcntB;
+    double* linvd;   // rows: pivot reciprocal in level order
+    double* rl;      // rows: right-hand side of the preconditioner in level order
+    int* fcolP;      // PC_MAXE * rowsCap
+    double* fvalP;
+    int* bcolP;
+    double* bvalP;
+    size_t pcSmem;   // its dynamic shared memory per CTA
     // PCG
     double* x;
     double* r;
@@ -61,8 +112,14 @@ void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWr
 void launch_dof_numbering(const Dev& d, const uint8_t* open, Proj& P, cudaStream_t st);
 void launch_assemble(const Dev& d, const Fields& F, const uint8_t* open, Proj& P, const int* hoPtr, const int* hoIdx,
                      double dt, cudaStream_t st);
-void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st);
-int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& epoch, int batch, cudaStream_t st);
+void launch_level_schedule(const Dev& d, Proj& P, cudaStream_t st);
+void launch_external_system(const Dev& d, Proj& P, int rows, cudaStream_t st);
+int choose_cluster_size(int device);
+int choose_dsmem_cluster(int maxRows, size_t* smemBytes);
+extern cudaError_t g_cluster_error;  // last failed cluster launch (cudaSuccess if none)
+void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st, KProf* prof);
+int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& epoch, int batch, cudaStream_t st,
+                    KProf* prof);
 void launch_pressure_update(const Dev& d, const Fields& F, const uint8_t* open, const int* pO, const int* pT,
                             const double* p, double dt, cudaStream_t st);
 void launch_dual(const Dev& d, const Fields& F, cudaStream_t st);

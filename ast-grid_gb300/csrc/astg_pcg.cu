@@ -12,10 +12,46 @@
 // rows are handed out in dependency order from an atomic counter and each row waits on per-row
 // ready flags of the rows it reads.  Every wait is bounded; on timeout the kernel records
 // DS_WAIT_TIMEOUT in the device status word and carries on, so a wait can never hang the GPU.
+#include <cooperative_groups.h>
+#include <cstdio>
+#include <cstdlib>
+
 #include "astg_launch.h"
 #include "astg_sample.cuh"
 
+namespace cg = cooperative_groups;
+
 namespace astg {
+
+long long g_launches = 0;
+
+// event pairs around profiled launches; drained after each host synchronisation
+static void prof_begin(KProf* p, int kind, cudaStream_t st) {
+    if (!p || !p->on) return;
+    if (!p->created) {
+        for (auto& e : p->ev) cudaEventCreate(&e);
+        p->created = true;
+    }
+    if (p->used >= 128) return;
+    p->kind[p->used] = kind;
+    cudaEventRecord(p->ev[2 * p->used], st);
+}
+static void prof_end(KProf* p, cudaStream_t st) {
+    if (!p || !p->on || p->used >= 128) return;
+    cudaEventRecord(p->ev[2 * p->used + 1], st);
+    ++p->used;
+}
+static void prof_drain(KProf* p) {
+    if (!p || !p->on) return;
+    for (int i = 0; i < p->used; ++i) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, p->ev[2 * i], p->ev[2 * i + 1]) == cudaSuccess) {
+            p->ms[p->kind[i]] += ms;
+            p->count[p->kind[i]] += 1;
+        }
+    }
+    p->used = 0;
+}
 
 constexpr int TB = 256;
 static inline int nblk(long long n) { return (int)((n + TB - 1) / TB); }
@@ -93,9 +129,9 @@ void launch_mean_temperature(const Dev& d, const double* hO, double* parts, cons
     for (int l = 0; l < d.L; ++l) {
         long long n = d.lN[l] + d.lG[l];
         int m = partOffHost[l + 1] - partOffHost[l];
-        if (m > 0) k_tree_sum<<<m, RED_LANES, 0, st>>>(hO + d.loff[l], nullptr, n, parts + partOffHost[l]);
+        if (m > 0) ASTG_LAUNCH(k_tree_sum<<<m, RED_LANES, 0, st>>>(hO + d.loff[l], nullptr, n, parts + partOffHost[l]));
     }
-    k_amb<<<1, RED_LANES, 0, st>>>(d, parts, partOffDev, amb);
+    ASTG_LAUNCH(k_amb<<<1, RED_LANES, 0, st>>>(d, parts, partOffDev, amb));
 }
 
 // ------------------------------------------------------------------ exclusive scan (int)
@@ -115,15 +151,28 @@ __global__ void k_scan_block(const int* in, int* out, int* bsum, long long n) {
     if (i < n) out[i] = sh[threadIdx.x] - v;
     if (threadIdx.x == SCAN_B - 1) bsum[blockIdx.x] = sh[threadIdx.x];
 }
+// exclusive scan of the block sums by one block: each thread scans a contiguous run
 __global__ void k_scan_sums(int* bsum, int nb, int* total) {
-    if (threadIdx.x != 0) return;
-    int acc = 0;
-    for (int b = 0; b < nb; ++b) {
-        int v = bsum[b];
-        bsum[b] = acc;
-        acc += v;
+    __shared__ int sh[SCAN_B];
+    int per = (nb + SCAN_B - 1) / SCAN_B;
+    int t = threadIdx.x, a = t * per, b = min(a + per, nb);
+    int s = 0;
+    for (int i = a; i < b; ++i) s += bsum[i];
+    sh[t] = s;
+    __syncthreads();
+    for (int off = 1; off < SCAN_B; off <<= 1) {
+        int v = t >= off ? sh[t - off] : 0;
+        __syncthreads();
+        sh[t] += v;
+        __syncthreads();
     }
-    *total = acc;
+    int run = sh[t] - s;
+    for (int i = a; i < b; ++i) {
+        int v = bsum[i];
+        bsum[i] = run;
+        run += v;
+    }
+    if (t == SCAN_B - 1) *total = sh[t];
 }
 __global__ void k_scan_add(int* out, const int* bsum, long long n) {
     long long i = (long long)blockIdx.x * SCAN_B + threadIdx.x;
@@ -132,9 +181,9 @@ __global__ void k_scan_add(int* out, const int* bsum, long long n) {
 // out = exclusive scan of in[0..n); *total = sum.  bsum needs ceil(n/1024) ints.
 static void exclusive_scan(const int* in, int* out, int* bsum, int* total, long long n, cudaStream_t st) {
     int nb = (int)((n + SCAN_B - 1) / SCAN_B);
-    k_scan_block<<<nb, SCAN_B, 0, st>>>(in, out, bsum, n);
-    k_scan_sums<<<1, 32, 0, st>>>(bsum, nb, total);
-    k_scan_add<<<nb, SCAN_B, 0, st>>>(out, bsum, n);
+    ASTG_LAUNCH(k_scan_block<<<nb, SCAN_B, 0, st>>>(in, out, bsum, n));
+    ASTG_LAUNCH(k_scan_sums<<<1, SCAN_B, 0, st>>>(bsum, nb, total));
+    ASTG_LAUNCH(k_scan_add<<<nb, SCAN_B, 0, st>>>(out, bsum, n));
 }
 
 // ------------------------------------------------------------------ DOF numbering
@@ -175,12 +224,12 @@ __global__ void k_dof_ghost(Dev d, int* pT, int l) {
     }
 }
 void launch_dof_numbering(const Dev& d, const uint8_t* open, Proj& P, cudaStream_t st) {
-    k_dof_count<<<nblk(d.S), TB, 0, st>>>(d, open, P.cnt);
+    ASTG_LAUNCH(k_dof_count<<<nblk(d.S), TB, 0, st>>>(d, open, P.cnt));
     exclusive_scan(P.cnt, P.base, P.bsum, P.n0, d.S, st);
-    k_dof_assign<<<nblk(d.S), TB, 0, st>>>(d, open, P.base, P.pO, P.pT);
-    k_dof_half<<<nblk(d.H > 0 ? d.H : 1), TB, 0, st>>>(d, P.pT, P.n0, P.nDof);
+    ASTG_LAUNCH(k_dof_assign<<<nblk(d.S), TB, 0, st>>>(d, open, P.base, P.pO, P.pT));
+    ASTG_LAUNCH(k_dof_half<<<nblk(d.H > 0 ? d.H : 1), TB, 0, st>>>(d, P.pT, P.n0, P.nDof));
     for (int l = 0; l < d.L; ++l)
-        if (d.lG[l]) k_dof_ghost<<<nblk(d.lG[l]), TB, 0, st>>>(d, P.pT, l);
+        if (d.lG[l]) ASTG_LAUNCH(k_dof_ghost<<<nblk(d.lG[l]), TB, 0, st>>>(d, P.pT, l));
 }
 
 // ------------------------------------------------------------------ assembly
@@ -439,6 +488,20 @@ __global__ void k_transpose_map(const Dev d, Proj P) {
         P.tpos[q] = t;
     }
 }
+// diagonal positions of a caller-supplied CSR matrix (astg_solve); a row without one is reported
+__global__ void k_find_diag(const Dev d, Proj P) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= *P.nDof) return;
+    int dg = -1;
+    for (int q = P.rowPtr[r]; q < P.rowPtr[r + 1]; ++q)
+        if (P.col[q] == r) dg = q;
+    if (dg < 0) report(d, DS_MISSING_NODE);
+    P.diagPos[r] = dg;
+}
+void launch_external_system(const Dev& d, Proj& P, int rows, cudaStream_t st) {
+    ASTG_LAUNCH(k_find_diag<<<nblk(rows), TB, 0, st>>>(d, P));
+    ASTG_LAUNCH(k_transpose_map<<<nblk(rows), TB, 0, st>>>(d, P));
+}
 __global__ void k_zero_rows(Proj P, int maxRows) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r < maxRows) { P.rowCnt[r] = 0; P.bRaw[r] = 0; }
@@ -446,14 +509,14 @@ __global__ void k_zero_rows(Proj P, int maxRows) {
 void launch_assemble(const Dev& d, const Fields& F, const uint8_t* open, Proj& P, const int* hoPtr, const int* hoIdx,
                      double dt, cudaStream_t st) {
     int maxRows = d.S + d.H;
-    k_zero_rows<<<nblk(maxRows), TB, 0, st>>>(P, maxRows);
-    k_asm_oct<<<nblk(d.S), TB, 0, st>>>(d, F, P, hoPtr, hoIdx);
-    k_asm_tilt<<<nblk(d.S), TB, 0, st>>>(d, F, P, open);
-    if (d.H) k_asm_half<<<nblk(d.H), TB, 0, st>>>(d, F, P);
+    ASTG_LAUNCH(k_zero_rows<<<nblk(maxRows), TB, 0, st>>>(P, maxRows));
+    ASTG_LAUNCH(k_asm_oct<<<nblk(d.S), TB, 0, st>>>(d, F, P, hoPtr, hoIdx));
+    ASTG_LAUNCH(k_asm_tilt<<<nblk(d.S), TB, 0, st>>>(d, F, P, open));
+    if (d.H) ASTG_LAUNCH(k_asm_half<<<nblk(d.H), TB, 0, st>>>(d, F, P));
     exclusive_scan(P.rowCnt, P.rowPtr, P.bsum, P.nnz, maxRows, st);
-    k_rowptr_last<<<1, 1, 0, st>>>(P);
-    k_csr_fill<<<nblk(maxRows), TB, 0, st>>>(P, d.rho / dt);
-    k_transpose_map<<<nblk(maxRows), TB, 0, st>>>(d, P);
+    ASTG_LAUNCH(k_rowptr_last<<<1, 1, 0, st>>>(P));
+    ASTG_LAUNCH(k_csr_fill<<<nblk(maxRows), TB, 0, st>>>(P, d.rho / dt));
+    ASTG_LAUNCH(k_transpose_map<<<nblk(maxRows), TB, 0, st>>>(d, P));
 }
 
 // ------------------------------------------------------------------ sync-free helpers
@@ -500,10 +563,12 @@ __global__ void k_mic_factor(Dev d, Proj P, double omega, double minDiag, int ep
         int dgj = P.diagPos[j];
         int upj = dgj >= 0 ? dgj + 1 : rj1;  // first entry of column j of L
         double invd = P.invdiag[j];
+        int lev = 0;
         for (int qq = rj0; qq < rj1; ++qq) {
             int k = P.col[qq];
             if (k >= j) break;
             wait_flag(d, P.ready + k, epoch);
+            lev = max(lev, P.level[k] + 1);
             if (P.adiag[k] == 0) continue;
             int tq = P.tpos[qq];  // entry (k, j): L(j, k)
             double mult = P.Lv[tq];
@@ -536,9 +601,368 @@ __global__ void k_mic_factor(Dev d, Proj P, double omega, double minDiag, int ep
             for (int q = upj; q < rj1; ++q) P.Lv[q] *= invd;
         }
         P.invdiag[j] = invd;
+        P.level[j] = lev;
         __threadfence();
         st_flag(P.ready + j, epoch);
     }
+}
+
+// ------------------------------------------------------------------ level schedule
+// Rows grouped by dependency depth: a row of level g reads only rows of levels < g in the
+// forward sweep and only rows of levels > g in the backward sweep, so rows of one level are
+// independent in both.  The order inside a level does not change any result.
+__global__ void k_level_hist(Proj P) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *P.nDof) return;
+    int g = P.level[j];
+    atomicAdd(P.levelCnt + g, 1);
+    atomicMax(P.nLevels, g + 1);
+}
+__global__ void k_level_scatter(Proj P) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *P.nDof) return;
+    int g = P.level[j];
+    P.perm[P.levelPtr[g] + atomicAdd(P.fill + g, 1)] = j;
+}
+__global__ void k_level_counts(Proj P) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= *P.nDof) return;
+    int i = P.perm[p];
+    int dg = P.diagPos[i];
+    P.cntF[p] = dg - P.rowPtr[i];
+    P.cntB[p] = P.rowPtr[i + 1] - dg - 1;
+}
+__global__ void k_level_fill(Proj P) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= *P.nDof) return;
+    int i = P.perm[p];
+    int dg = P.diagPos[i];
+    if (P.fcolP) {
+        int cap = P.rowsCap;
+        P.pos[i] = p;
+        P.linvd[p] = P.invdiag[i];
+        int nf = dg - P.rowPtr[i], nb = P.rowPtr[i + 1] - dg - 1;
+        P.lcntF[p] = nf;
+        P.lcntB[p] = nb;
+        for (int e = 0; e < PC_MAXE; ++e) {
+            int qf = P.rowPtr[i] + e, qb = dg + 1 + e;
+            P.fcolP[(size_t)e * cap + p] = e < nf ? P.col[qf] : 0;
+            P.fvalP[(size_t)e * cap + p] = e < nf ? P.Lv[P.tpos[qf]] : 0.0;
+            P.bcolP[(size_t)e * cap + p] = e < nb ? P.col[qb] : 0;
+            P.bvalP[(size_t)e * cap + p] = e < nb ? P.Lv[qb] : 0.0;
+        }
+    }
+    int o = P.fptr[p];
+    for (int q = P.rowPtr[i]; q < dg; ++q, ++o) {
+        P.fcol[o] = P.col[q];
+        P.fval[o] = P.Lv[P.tpos[q]];  // L(i, k), held in column k's storage
+    }
+    o = P.bptr[p];
+    for (int q = dg + 1; q < P.rowPtr[i + 1]; ++q, ++o) {
+        P.bcol[o] = P.col[q];
+        P.bval[o] = P.Lv[q];
+    }
+}
+__global__ void k_level_fptr_last(Proj P) {
+    int n = *P.nDof;
+    P.fptr[n] = P.nnz[2];
+    P.bptr[n] = P.nnz[3];
+}
+__global__ void k_level_reset(Proj P, int rows) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j <= rows) { P.levelCnt[j] = 0; P.fill[j] = 0; }
+    if (j == 0) *P.nLevels = 0;
+}
+
+// ------------------------------------------------------------------ cluster sweeps
+constexpr int CLUSTER_THREADS = 512;
+constexpr int PC_THREADS = 256;
+cudaError_t g_cluster_error = cudaSuccess;
+// One thread-block cluster walks the levels; a hardware cluster barrier (release/acquire at
+// cluster scope) separates consecutive levels, so no row ever polls a flag.  Per row the
+// operations are the reference's, in the same order.
+__global__ void k_sweep_fwd_cluster(Proj P, const double* r, double* z) {
+    if (*P.done) return;
+    cg::cluster_group cl = cg::this_cluster();
+    int nth = cl.num_blocks() * blockDim.x;
+    int t = cl.block_rank() * blockDim.x + threadIdx.x;
+    int nl = *P.nLevels;
+    for (int g = 0; g < nl; ++g) {
+        int p1 = P.levelPtr[g + 1];
+        for (int p = P.levelPtr[g] + t; p < p1; p += nth) {
+            int i = P.perm[p];
+            double acc = r[i];
+            for (int q = P.fptr[p]; q < P.fptr[p + 1]; ++q) acc = acc - P.fval[q] * __ldcg(z + P.fcol[q]);
+            z[i] = acc * P.invdiag[i];
+        }
+        cl.sync();
+    }
+}
+__global__ void k_sweep_bwd_cluster(Proj P, const double* unused, double* z) {
+    (void)unused;
+    if (*P.done) return;
+    cg::cluster_group cl = cg::this_cluster();
+    int nth = cl.num_blocks() * blockDim.x;
+    int t = cl.block_rank() * blockDim.x + threadIdx.x;
+    int nl = *P.nLevels;
+    for (int g = nl - 1; g >= 0; --g) {
+        int p1 = P.levelPtr[g + 1];
+        for (int p = P.levelPtr[g] + t; p < p1; p += nth) {
+            int i = P.perm[p];
+            double acc = __ldcg(z + i);
+            for (int q = P.bptr[p]; q < P.bptr[p + 1]; ++q) acc = acc - P.bval[q] * __ldcg(z + P.bcol[q]);
+            z[i] = acc * P.invdiag[i];
+        }
+        cl.sync();
+    }
+}
+// Both sweeps in one cluster launch with the vector held in distributed shared memory: entry i
+// lives in CTA (i & (CS-1)) at index (i >> log2 CS).  Each thread owns at most one row of a level
+// (rows beyond blockDim * CS take a slower loop).  While the cluster barrier between two levels is
+// in flight, every thread already loads the next level's row (index, right-hand side, pivot and
+// up to PC_MAXE factor entries) into registers, so after the barrier only the DSMEM reads of
+// finished entries remain on the critical path.  Per row the operations are the reference's, in
+// the reference's order.
+__device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+__device__ __forceinline__ double ld_ds(uint32_t a) {
+    double v;
+    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_ds(uint32_t a, double v) {
+    asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+struct PcRow {
+    int i, p, cnt;
+    double rhs, invd;
+    int col[PC_MAXE];
+    double val[PC_MAXE];
+};
+// record of level position p (p < p1): independent loads only
+__device__ __forceinline__ void pc_load(const Proj& P, int p, int p1, bool fwd, PcRow& w) {
+    w.cnt = -1;
+    if (p >= p1) return;
+    const int cap = P.rowsCap;
+    const int* cc = fwd ? P.fcolP : P.bcolP;
+    const double* vv = fwd ? P.fvalP : P.bvalP;
+    w.p = p;
+    w.i = P.perm[p];
+    w.cnt = fwd ? P.lcntF[p] : P.lcntB[p];
+    w.invd = P.linvd[p];
+    w.rhs = fwd ? P.rl[p] : 0.0;
+#pragma unroll
+    for (int e = 0; e < PC_MAXE; ++e) {
+        w.col[e] = cc[(size_t)e * cap + p];
+        w.val[e] = vv[(size_t)e * cap + p];
+    }
+}
+// row i lives in CTA (i & msk) of the cluster at local index (i >> lg)
+__device__ __forceinline__ void pc_row(const Proj& P, const PcRow& w, bool fwd, const uint32_t* rb, int lg, int msk) {
+    uint32_t ai = rb[w.i & msk] + (uint32_t)(w.i >> lg) * 8u;
+    double zk[PC_MAXE];
+#pragma unroll
+    for (int e = 0; e < PC_MAXE; ++e)
+        if (e < w.cnt) zk[e] = ld_ds(rb[w.col[e] & msk] + (uint32_t)(w.col[e] >> lg) * 8u);
+    double acc = fwd ? w.rhs : ld_ds(ai);
+#pragma unroll
+    for (int e = 0; e < PC_MAXE; ++e)
+        if (e < w.cnt) acc = acc - w.val[e] * zk[e];
+    if (w.cnt > PC_MAXE) {  // rows longer than the padded record: the rest from the compact arrays
+        const int* cc = fwd ? P.fcol : P.bcol;
+        const double* vv = fwd ? P.fval : P.bval;
+        int q0 = (fwd ? P.fptr : P.bptr)[w.p];
+        for (int e = PC_MAXE; e < w.cnt; ++e) {
+            int k = cc[q0 + e];
+            acc = acc - vv[q0 + e] * ld_ds(rb[k & msk] + (uint32_t)(k >> lg) * 8u);
+        }
+    }
+    st_ds(ai, acc * w.invd);
+}
+constexpr int PC_MAX_LEVELS = 4096;  // level bounds staged in shared memory
+__device__ __forceinline__ void pc_level(const Proj& P, const PcRow& w, bool fwd, const uint32_t* rb, int lg, int msk,
+                                         int p0, int p1, int t, int nth) {
+    if (w.cnt >= 0) pc_row(P, w, fwd, rb, lg, msk);
+    for (int p = p0 + t + nth; p < p1; p += nth) {  // levels wider than the cluster
+        PcRow x;
+        pc_load(P, p, p1, fwd, x);
+        pc_row(P, x, fwd, rb, lg, msk);
+    }
+    __syncwarp();  // the .aligned cluster barrier needs converged warps
+    cl_arrive();
+}
+// Both MIC(0) triangular sweeps of one preconditioner application in one cluster launch.  z lives
+// in the CTAs' shared memory (row i in CTA i mod CS), every level is one split cluster barrier,
+// and the next levels' records are loaded into registers while the barrier completes.
+__global__ void __launch_bounds__(256, 1) k_precond_dsmem(Proj P, double* z, int lgCS) {
+    if (*P.done) return;
+    extern __shared__ double zsh[];
+    __shared__ uint32_t rb[16];
+    __shared__ int lp[PC_MAX_LEVELS + 1];
+    cg::cluster_group cl = cg::this_cluster();
+    const int msk = (1 << lgCS) - 1;
+    const int rank = cl.block_rank();
+    const int nth = blockDim.x << lgCS;
+    const int t = rank * blockDim.x + threadIdx.x;
+    const int nl = *P.nLevels;
+    if (threadIdx.x < (1 << lgCS)) {
+        uint32_t a = (uint32_t)__cvta_generic_to_shared(zsh), m;
+        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(m) : "r"(a), "r"((uint32_t)threadIdx.x));
+        rb[threadIdx.x] = m;
+    }
+    for (int g = threadIdx.x; g <= nl && g <= PC_MAX_LEVELS; g += blockDim.x) lp[g] = P.levelPtr[g];
+    cl.sync();  // every CTA of the cluster is running; rb and lp are set
+    // level bounds (staged in shared memory up to PC_MAX_LEVELS levels)
+    auto LP = [&](int g) { return g <= PC_MAX_LEVELS ? lp[g] : P.levelPtr[g]; };
+    for (int dir = 0; dir < 2; ++dir) {
+        const bool fwd = dir == 0;
+        // level of step k: k (forward) or nl-1-k (backward); rows of step k+2 are fetched while
+        // step k+1 waits at the barrier, so the loads have two steps to arrive
+        auto lvl = [&](int k) { return fwd ? k : nl - 1 - k; };
+        PcRow A, B;
+        pc_load(P, LP(lvl(0)) + t, LP(lvl(0) + 1), fwd, A);
+        if (nl > 1) pc_load(P, LP(lvl(1)) + t, LP(lvl(1) + 1), fwd, B);
+        for (int k = 0; k < nl; k += 2) {
+            int g = lvl(k);
+            pc_level(P, A, fwd, rb, lgCS, msk, LP(g), LP(g + 1), t, nth);
+            if (k + 2 < nl) pc_load(P, LP(lvl(k + 2)) + t, LP(lvl(k + 2) + 1), fwd, A);
+            __syncwarp();
+            cl_wait();
+            if (k + 1 < nl) {
+                g = lvl(k + 1);
+                pc_level(P, B, fwd, rb, lgCS, msk, LP(g), LP(g + 1), t, nth);
+                if (k + 3 < nl) pc_load(P, LP(lvl(k + 3)) + t, LP(lvl(k + 3) + 1), fwd, B);
+                __syncwarp();
+                cl_wait();
+            }
+        }
+    }
+    int n = *P.nDof;
+    for (int j = threadIdx.x; (j << lgCS) + rank < n; j += blockDim.x) z[(j << lgCS) + rank] = zsh[j];
+    cl.sync();
+}
+static cudaError_t launch_precond_dsmem(const Proj& P, const double* r, double* z, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(P.pcCluster);
+    cfg.blockDim = dim3(PC_THREADS);
+    cfg.dynamicSmemBytes = P.pcSmem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = P.pcCluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int lg = 0;
+    while ((1 << lg) < P.pcCluster) ++lg;
+    ++g_launches;
+    (void)r;
+    return cudaLaunchKernelEx(&cfg, k_precond_dsmem, P, z, lg);
+}
+// cluster size (16 or 8) whose distributed shared memory holds a vector of maxRows doubles, or 0
+int choose_dsmem_cluster(int maxRows, size_t* smemBytes) {
+    cudaFuncSetAttribute((const void*)k_precond_dsmem, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    // the attribute is process-wide: allow the device maximum once (minus the kernel's static
+    // shared memory), size each launch per handle
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, (const void*)k_precond_dsmem) != cudaSuccess) {
+        cudaGetLastError();
+        *smemBytes = 0;
+        return 0;
+    }
+    optin -= (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute((const void*)k_precond_dsmem, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        *smemBytes = 0;
+        return 0;
+    }
+    for (int cs : {16, 8}) {
+        size_t bytes = (size_t)((maxRows + cs - 1) / cs) * sizeof(double);
+        if (bytes > (size_t)optin) continue;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(PC_THREADS);
+        cfg.dynamicSmemBytes = bytes;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        cudaError_t e = cudaOccupancyMaxActiveClusters(&nc, (const void*)k_precond_dsmem, &cfg);
+        if (getenv("ASTG_VERBOSE"))
+            fprintf(stderr, "astg: DSMEM preconditioner cluster %d, %zu B smem/CTA: %d clusters (%s)\n", cs, bytes, nc,
+                    cudaGetErrorString(e));
+        if (e == cudaSuccess && nc > 0) {
+            *smemBytes = bytes;
+            return cs;
+        }
+        cudaGetLastError();
+    }
+    *smemBytes = 0;
+    return 0;
+}
+static cudaError_t launch_cluster(void (*kern)(Proj, const double*, double*), int csize, cudaStream_t st, Proj P,
+                                  const double* r, double* z) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(csize);
+    cfg.blockDim = dim3(CLUSTER_THREADS);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    ++g_launches;
+    return cudaLaunchKernelEx(&cfg, kern, P, r, z);
+}
+// largest cluster size (16, 8, 4, 2) that can be resident for the sweep kernels
+int choose_cluster_size(int device) {
+    (void)device;
+    cudaFuncSetAttribute((const void*)k_sweep_fwd_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute((const void*)k_sweep_bwd_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (int cs : {16, 8, 4, 2}) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(CLUSTER_THREADS);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, (const void*)k_sweep_fwd_cluster, &cfg) == cudaSuccess && nc > 0) {
+            int nc2 = 0;
+            if (cudaOccupancyMaxActiveClusters(&nc2, (const void*)k_sweep_bwd_cluster, &cfg) == cudaSuccess && nc2 > 0)
+                return cs;
+        }
+        cudaGetLastError();
+    }
+    return 0;
+}
+void launch_level_schedule(const Dev& d, Proj& P, cudaStream_t st) {
+    int maxRows = d.S + d.H;
+    ASTG_LAUNCH(k_level_reset<<<nblk(maxRows + 1), TB, 0, st>>>(P, maxRows));
+    ASTG_LAUNCH(k_level_hist<<<nblk(maxRows), TB, 0, st>>>(P));
+
+    exclusive_scan(P.levelCnt, P.levelPtr, P.bsum, P.nnz + 1, maxRows + 1, st);
+    ASTG_LAUNCH(k_level_scatter<<<nblk(maxRows), TB, 0, st>>>(P));
+    ASTG_LAUNCH(k_level_counts<<<nblk(maxRows), TB, 0, st>>>(P));
+    exclusive_scan(P.cntF, P.fptr, P.bsum, P.nnz + 2, maxRows, st);
+    exclusive_scan(P.cntB, P.bptr, P.bsum, P.nnz + 3, maxRows, st);
+    ASTG_LAUNCH(k_level_fptr_last<<<1, 1, 0, st>>>(P));
+    ASTG_LAUNCH(k_level_fill<<<nblk(maxRows), TB, 0, st>>>(P));
 }
 
 // ------------------------------------------------------------------ triangular sweeps (FP64)
@@ -591,6 +1015,11 @@ __global__ void k_sweep_bwd(Dev d, Proj P, double* z, int epoch) {
 __global__ void k_copy(const double* a, double* b, const int* nptr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < *nptr) b[i] = a[i];
+}
+// right-hand side of the preconditioner in level order
+__global__ void k_to_level_order(Proj P, const double* r) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *P.nDof) P.rl[P.pos[i]] = r[i];
 }
 __global__ void k_zero_vec(double* a, const int* nptr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -662,6 +1091,7 @@ __global__ void k_update_xr(Proj P, double* x, double* r, const double* s, const
         x[i] += alpha * s[i];
         double ri = r[i] + -alpha * z[i];
         r[i] = ri;
+        if (P.pcCluster) P.rl[P.pos[i]] = ri;
         v = fabs(ri);
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -708,58 +1138,86 @@ __global__ void k_update_s(Proj P, double* s, const double* z) {
 __global__ void k_reset_counter(int* c) { *c = 0; }
 
 // one preconditioner application z = (L L^T)^-1 r
-static void precond(const Dev& d, Proj& P, const double* r, double* z, int& epoch, int rowsMax, cudaStream_t st) {
+static void precond(const Dev& d, Proj& P, const double* r, double* z, int& epoch, cudaStream_t st, KProf* prof) {
+    if (P.pcCluster > 0) {
+        prof_begin(prof, 0, st);
+        cudaError_t e = launch_precond_dsmem(P, r, z, st);
+        prof_end(prof, st);
+        if (e != cudaSuccess) g_cluster_error = e;
+        return;
+    }
+    if (P.clusterSize > 0) {
+        prof_begin(prof, 0, st);
+        cudaError_t e = launch_cluster(k_sweep_fwd_cluster, P.clusterSize, st, P, r, z);
+        prof_end(prof, st);
+        prof_begin(prof, 1, st);
+        cudaError_t e2 = launch_cluster(k_sweep_bwd_cluster, P.clusterSize, st, P, nullptr, z);
+        prof_end(prof, st);
+        if (e != cudaSuccess) g_cluster_error = e;
+        if (e2 != cudaSuccess) g_cluster_error = e2;
+        return;
+    }
     int warps = P.sweepBlocks;
-    k_reset_counter<<<1, 1, 0, st>>>(P.counter);
-    k_sweep_fwd<<<warps, 128, 0, st>>>(d, P, r, z, ++epoch);
-    k_reset_counter<<<1, 1, 0, st>>>(P.counter);
-    k_sweep_bwd<<<warps, 128, 0, st>>>(d, P, z, ++epoch);
-    (void)rowsMax;
+    ASTG_LAUNCH(k_reset_counter<<<1, 1, 0, st>>>(P.counter));
+    prof_begin(prof, 0, st);
+    ASTG_LAUNCH(k_sweep_fwd<<<warps, 128, 0, st>>>(d, P, r, z, ++epoch));
+    prof_end(prof, st);
+    ASTG_LAUNCH(k_reset_counter<<<1, 1, 0, st>>>(P.counter));
+    prof_begin(prof, 1, st);
+    ASTG_LAUNCH(k_sweep_bwd<<<warps, 128, 0, st>>>(d, P, z, ++epoch));
+    prof_end(prof, st);
 }
 
-void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st) {
+void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st, KProf* prof) {
     int maxRows = d.S + d.H;
-    k_mic_init<<<nblk(maxRows), TB, 0, st>>>(P);
-    k_reset_counter<<<1, 1, 0, st>>>(P.counter);
-    k_mic_factor<<<P.sweepBlocks, 128, 0, st>>>(d, P, omega, minDiag, ++epoch);
+    ASTG_LAUNCH(k_mic_init<<<nblk(maxRows), TB, 0, st>>>(P));
+    ASTG_LAUNCH(k_reset_counter<<<1, 1, 0, st>>>(P.counter));
+    prof_begin(prof, 3, st);
+    ASTG_LAUNCH(k_mic_factor<<<P.sweepBlocks, 128, 0, st>>>(d, P, omega, minDiag, ++epoch));
+    prof_end(prof, st);
 }
 
 // Runs the FP64 PCG to completion.  Iterations are launched in batches; every kernel returns at
 // once when the device "done" flag is set, so a batch that overshoots does no work.
-int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& epoch, int batch, cudaStream_t st) {
+int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& epoch, int batch, cudaStream_t st,
+                    KProf* prof) {
     int maxRows = d.S + d.H;
     int chunks = (maxRows + RED_CHUNK - 1) / RED_CHUNK;
     double* x = P.x;
     double* r = P.r;
     double* s = P.s;
     double* z = P.z;
-    k_zero_vec<<<nblk(maxRows), TB, 0, st>>>(x, P.nDof);
-    k_copy<<<nblk(maxRows), TB, 0, st>>>(P.b, r, P.nDof);
+    ASTG_LAUNCH(k_zero_vec<<<nblk(maxRows), TB, 0, st>>>(x, P.nDof));
+    ASTG_LAUNCH(k_copy<<<nblk(maxRows), TB, 0, st>>>(P.b, r, P.nDof));
     cudaMemsetAsync(P.amax, 0, sizeof(unsigned long long), st);
     cudaMemsetAsync(P.done, 0, sizeof(int), st);
-    k_absmax<<<nblk(maxRows), TB, 0, st>>>(r, P.nDof, P.amax);
-    precond(d, P, r, z, epoch, maxRows, st);
-    k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part);
-    k_pcg_start<<<1, RED_LANES, 0, st>>>(P, P.part, tolFactor);
-    k_copy<<<nblk(maxRows), TB, 0, st>>>(z, s, P.nDof);
+    ASTG_LAUNCH(k_absmax<<<nblk(maxRows), TB, 0, st>>>(r, P.nDof, P.amax));
+    if (P.pcCluster) ASTG_LAUNCH(k_to_level_order<<<nblk(maxRows), TB, 0, st>>>(P, r));
+    precond(d, P, r, z, epoch, st, prof);
+    ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
+    ASTG_LAUNCH(k_pcg_start<<<1, RED_LANES, 0, st>>>(P, P.part, tolFactor));
+    ASTG_LAUNCH(k_copy<<<nblk(maxRows), TB, 0, st>>>(z, s, P.nDof));
     int launched = 0;
     int hostDone = 0;
     while (launched < maxIter) {
         int nb = batch;
         if (launched + nb > maxIter) nb = maxIter - launched;
         for (int it = 0; it < nb; ++it) {
-            k_spmv_dot<<<chunks, RED_LANES, 0, st>>>(P, s, z, P.part);
-            k_alpha<<<1, RED_LANES, 0, st>>>(P, P.part);
-            k_update_xr<<<nblk(maxRows), TB, 0, st>>>(P, x, r, s, z);
-            k_check<<<1, 1, 0, st>>>(P, maxIter);
-            precond(d, P, r, z, epoch, maxRows, st);
-            k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part);
-            k_beta<<<1, RED_LANES, 0, st>>>(P, P.part);
-            k_update_s<<<nblk(maxRows), TB, 0, st>>>(P, s, z);
+            prof_begin(prof, 2, st);
+            ASTG_LAUNCH(k_spmv_dot<<<chunks, RED_LANES, 0, st>>>(P, s, z, P.part));
+            prof_end(prof, st);
+            ASTG_LAUNCH(k_alpha<<<1, RED_LANES, 0, st>>>(P, P.part));
+            ASTG_LAUNCH(k_update_xr<<<nblk(maxRows), TB, 0, st>>>(P, x, r, s, z));
+            ASTG_LAUNCH(k_check<<<1, 1, 0, st>>>(P, maxIter));
+            precond(d, P, r, z, epoch, st, prof);
+            ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
+            ASTG_LAUNCH(k_beta<<<1, RED_LANES, 0, st>>>(P, P.part));
+            ASTG_LAUNCH(k_update_s<<<nblk(maxRows), TB, 0, st>>>(P, s, z));
         }
         launched += nb;
         cudaMemcpyAsync(P.hostDone, P.done, sizeof(int), cudaMemcpyDeviceToHost, st);
         cudaStreamSynchronize(st);
+        prof_drain(prof);
         hostDone = *P.hostDone;
         if (hostDone) break;
     }

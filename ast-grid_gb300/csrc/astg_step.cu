@@ -167,14 +167,14 @@ struct Vec3Acc {
 template <class T, class A>
 static void omni_ghost(const Dev& d, A oct, A til, const double* te, const uint32_t* tf, cudaStream_t st) {
     for (int l = 0; l < d.L; ++l)
-        if (d.lG[l]) k_cell_ghost_avg<T, A><<<nblk(d.lG[l]), TB, 0, st>>>(d, oct, l);
+        if (d.lG[l]) ASTG_LAUNCH(k_cell_ghost_avg<T, A><<<nblk(d.lG[l]), TB, 0, st>>>(d, oct, l));
     for (int l = 0; l < d.L; ++l)
-        if (d.lG[l]) k_cell_ghost_sample<T, A><<<nblk(d.lG[l]), TB, 0, st>>>(d, oct, l);
-    k_vertex_ghost<T, A><<<nblk(d.S), TB, 0, st>>>(d, til);
+        if (d.lG[l]) ASTG_LAUNCH(k_cell_ghost_sample<T, A><<<nblk(d.lG[l]), TB, 0, st>>>(d, oct, l));
+    ASTG_LAUNCH(k_vertex_ghost<T, A><<<nblk(d.S), TB, 0, st>>>(d, til));
     for (int l = 0; l < d.L; ++l)
-        if (d.lG[l]) k_cell_ghost_joint<T, A><<<nblk(d.lG[l]), TB, 0, st>>>(d, oct, til, l);
-    if (d.nTJ) k_closed_joint<T, A><<<nblk(d.nTJ), TB, 0, st>>>(d, oct, til, te);
-    if (d.nCBH) k_closed_by_half<T, A><<<nblk(d.nCBH), TB, 0, st>>>(d, oct, til, tf);
+        if (d.lG[l]) ASTG_LAUNCH(k_cell_ghost_joint<T, A><<<nblk(d.lG[l]), TB, 0, st>>>(d, oct, til, l));
+    if (d.nTJ) ASTG_LAUNCH(k_closed_joint<T, A><<<nblk(d.nTJ), TB, 0, st>>>(d, oct, til, te));
+    if (d.nCBH) ASTG_LAUNCH(k_closed_by_half<T, A><<<nblk(d.nCBH), TB, 0, st>>>(d, oct, til, tf));
 }
 
 void launch_scalar_ghost(const Dev& d, double* oct, double* til, const double* te, const uint32_t* tf, cudaStream_t st) {
@@ -185,8 +185,8 @@ void launch_dual_ghost(const Dev& d, const Fields& F, cudaStream_t st) {
 }
 
 void launch_source(const Dev& d, const Fields& F, cudaStream_t st) {
-    k_source_slots<<<nblk(d.S), TB, 0, st>>>(d, F);
-    if (d.H) k_source_half<<<nblk(d.H), TB, 0, st>>>(d, F);
+    ASTG_LAUNCH(k_source_slots<<<nblk(d.S), TB, 0, st>>>(d, F));
+    if (d.H) ASTG_LAUNCH(k_source_half<<<nblk(d.H), TB, 0, st>>>(d, F));
 }
 
 // ------------------------------------------------------------------ buoyancy
@@ -201,37 +201,39 @@ __global__ void k_force_mac(Dev d, Fields F, const double* amb, double dt) {
     double* w = F.mac + 2 * (size_t)d.S + s;
     *w = *w + dt * force_at(d, F, mac_pos(d, 2, s), *amb);
 }
+// one thread per (tilt, slot)
 __global__ void k_force_tilt(Dev d, Fields F, const uint8_t* open, const double* amb, double dt) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.S || ghost(d, s) || !open[s]) return;
-    double a = *amb;
-    V3 c = vert_pos(d, s);
-    double e = F.te[s];
-    double nf[8];
-    for (int k = 0; k < 8; ++k) nf[k] = tilt_up(k, 2) * force_at(d, F, tilt_pos(c, k, e), a);
-    for (int k = 0; k < 8; ++k) F.tv[(size_t)s * 8 + k] = F.tv[(size_t)s * 8 + k] + dt * nf[k];
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 8LL * d.S) return;
+    int s = (int)(idx >> 3), k = (int)(idx & 7);
+    if (ghost(d, s) || !open[s]) return;
+    double nf = tilt_up(k, 2) * force_at(d, F, tilt_pos(vert_pos(d, s), k, F.te[s]), *amb);
+    F.tv[(size_t)s * 8 + k] = F.tv[(size_t)s * 8 + k] + dt * nf;
 }
+// one thread per (half tilt, slot); slots the half tilt does not use get + dt * 0
 __global__ void k_force_half(Dev d, Fields F, const double* amb, double dt) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.H) return;
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 8LL * d.H) return;
+    int i = (int)(idx >> 3), k = (int)(idx & 7);
     int hs = d.half[i];
-    double a = *amb;
     int dir = tf_dir(F.tf[hs]);
-    double nf[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    V3 c = vert_pos(d, hs);
-    for (int q = 0; q < 5; ++q) {
-        int k = HALF_SLOT[dir][q];
+    int q = -1;
+    for (int j = 0; j < 5; ++j)
+        if (HALF_SLOT[dir][j] == k) q = j;
+    double nf = 0;
+    if (q >= 0) {
+        V3 c = vert_pos(d, hs);
         V3 p = (q == 4) ? c : tilt_pos(c, k, F.te[hs]);
-        double tf = force_at(d, F, p, a);
+        double tf = force_at(d, F, p, *amb);
         V3 dv = (q == 4) ? v3(HALF_DIR_POS[k][0], HALF_DIR_POS[k][1], HALF_DIR_POS[k][2]) : tilt_up3(k);
-        nf[k] = dot3(v3(0, 0, tf), dv);
+        nf = dot3(v3(0, 0, tf), dv);
     }
-    for (int k = 0; k < 8; ++k) F.tv[(size_t)hs * 8 + k] = F.tv[(size_t)hs * 8 + k] + dt * nf[k];
+    F.tv[(size_t)hs * 8 + k] = F.tv[(size_t)hs * 8 + k] + dt * nf;
 }
 void launch_force(const Dev& d, const Fields& F, const uint8_t* open, const double* amb, double dt, cudaStream_t st) {
-    k_force_mac<<<nblk(d.S), TB, 0, st>>>(d, F, amb, dt);
-    k_force_tilt<<<nblk(d.S), TB, 0, st>>>(d, F, open, amb, dt);
-    if (d.H) k_force_half<<<nblk(d.H), TB, 0, st>>>(d, F, amb, dt);
+    ASTG_LAUNCH(k_force_mac<<<nblk(d.S), TB, 0, st>>>(d, F, amb, dt));
+    ASTG_LAUNCH(k_force_tilt<<<nblk(8LL * d.S), TB, 0, st>>>(d, F, open, amb, dt));
+    if (d.H) ASTG_LAUNCH(k_force_half<<<nblk(8LL * d.H), TB, 0, st>>>(d, F, amb, dt));
 }
 
 // ------------------------------------------------------------------ walls and velocity ghosts
@@ -296,15 +298,15 @@ __global__ void k_tilt_ghost(Dev d, Fields F, int l) {
     for (int k = 0; k < 8; ++k) F.tv[(size_t)s * 8 + k] = F.tv[(size_t)src * 8 + k];
 }
 void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st) {
-    k_walls<<<nblk(d.S), TB, 0, st>>>(d, F.mac);
-    k_mac_ghost_zero<<<nblk(d.S), TB, 0, st>>>(d, F.mac);
+    ASTG_LAUNCH(k_walls<<<nblk(d.S), TB, 0, st>>>(d, F.mac));
+    ASTG_LAUNCH(k_mac_ghost_zero<<<nblk(d.S), TB, 0, st>>>(d, F.mac));
     for (int l = 0; l < d.L; ++l)
-        if (d.lG[l]) k_mac_ghost_sample<<<nblk(d.lG[l]), TB, 0, st>>>(d, F.mac, l, 0);
-    if (d.H) k_mac_from_half<<<nblk(d.H), TB, 0, st>>>(d, F, lastWriter);
+        if (d.lG[l]) ASTG_LAUNCH(k_mac_ghost_sample<<<nblk(d.lG[l]), TB, 0, st>>>(d, F.mac, l, 0));
+    if (d.H) ASTG_LAUNCH(k_mac_from_half<<<nblk(d.H), TB, 0, st>>>(d, F, lastWriter));
     for (int l = 0; l < d.L; ++l)
-        if (d.lG[l]) k_mac_ghost_sample<<<nblk(d.lG[l]), TB, 0, st>>>(d, F.mac, l, 1);
+        if (d.lG[l]) ASTG_LAUNCH(k_mac_ghost_sample<<<nblk(d.lG[l]), TB, 0, st>>>(d, F.mac, l, 1));
     for (int l = 0; l < d.L; ++l)
-        if (d.lG[l]) k_tilt_ghost<<<nblk(d.lG[l]), TB, 0, st>>>(d, F, l);
+        if (d.lG[l]) ASTG_LAUNCH(k_tilt_ghost<<<nblk(d.lG[l]), TB, 0, st>>>(d, F, l));
 }
 
 // ------------------------------------------------------------------ pressure-gradient update
@@ -391,9 +393,9 @@ __global__ void k_pu_half(Dev d, Fields F, const int* pO, const int* pT, const d
 }
 void launch_pressure_update(const Dev& d, const Fields& F, const uint8_t* open, const int* pO, const int* pT,
                             const double* p, double dt, cudaStream_t st) {
-    k_pu_mac<<<nblk(d.S), TB, 0, st>>>(d, F, pO, p, dt);
-    k_pu_tilt<<<nblk(d.S), TB, 0, st>>>(d, F, open, pO, pT, p, dt);
-    if (d.H) k_pu_half<<<nblk(d.H), TB, 0, st>>>(d, F, pO, pT, p, dt);
+    ASTG_LAUNCH(k_pu_mac<<<nblk(d.S), TB, 0, st>>>(d, F, pO, p, dt));
+    ASTG_LAUNCH(k_pu_tilt<<<nblk(d.S), TB, 0, st>>>(d, F, open, pO, pT, p, dt));
+    if (d.H) ASTG_LAUNCH(k_pu_half<<<nblk(d.H), TB, 0, st>>>(d, F, pO, pT, p, dt));
 }
 
 // ------------------------------------------------------------------ dual velocity
@@ -491,9 +493,9 @@ __global__ void k_dual_half(Dev d, Fields F) {
     o[0] = f.x; o[1] = f.y; o[2] = f.z;
 }
 void launch_dual(const Dev& d, const Fields& F, cudaStream_t st) {
-    k_dual_tilt<<<nblk(d.S), TB, 0, st>>>(d, F);
-    k_dual_oct<<<nblk(d.S), TB, 0, st>>>(d, F);
-    if (d.H) k_dual_half<<<nblk(d.H), TB, 0, st>>>(d, F);
+    ASTG_LAUNCH(k_dual_tilt<<<nblk(d.S), TB, 0, st>>>(d, F));
+    ASTG_LAUNCH(k_dual_oct<<<nblk(d.S), TB, 0, st>>>(d, F));
+    if (d.H) ASTG_LAUNCH(k_dual_half<<<nblk(d.H), TB, 0, st>>>(d, F));
     launch_dual_ghost(d, F, st);
 }
 
@@ -567,14 +569,14 @@ __global__ void k_te_ghost(Dev d, double* te, uint32_t* tf, int l) {
 }
 void launch_tilt_e_ghost(const Dev& d, double* te, uint32_t* tf, cudaStream_t st) {
     for (int l = 0; l < d.L; ++l)
-        if (d.lG[l]) k_te_ghost<<<nblk(d.lG[l]), TB, 0, st>>>(d, te, tf, l);
+        if (d.lG[l]) ASTG_LAUNCH(k_te_ghost<<<nblk(d.lG[l]), TB, 0, st>>>(d, te, tf, l));
 }
 void launch_adjust(const Dev& d, const Fields& cur, const Fields& nxt, uint8_t* open, uint8_t* fixedf, double dt,
                    cudaStream_t st) {
-    k_adjust_open<<<nblk(d.S), TB, 0, st>>>(d, cur, open, fixedf, dt);
+    ASTG_LAUNCH(k_adjust_open<<<nblk(d.S), TB, 0, st>>>(d, cur, open, fixedf, dt));
     for (int l = 0; l < d.L; ++l)
-        if (d.lG[l]) k_layout_ghost<<<nblk(d.lG[l]), TB, 0, st>>>(d, open, fixedf, l);
-    k_adjust_e<<<nblk(d.S), TB, 0, st>>>(d, nxt.te, nxt.tf, open, fixedf);
+        if (d.lG[l]) ASTG_LAUNCH(k_layout_ghost<<<nblk(d.lG[l]), TB, 0, st>>>(d, open, fixedf, l));
+    ASTG_LAUNCH(k_adjust_e<<<nblk(d.S), TB, 0, st>>>(d, nxt.te, nxt.tf, open, fixedf));
     launch_tilt_e_ghost(d, nxt.te, nxt.tf, st);
 }
 
@@ -604,41 +606,43 @@ __global__ void k_adv_scalar_half(Dev d, Fields cur, Fields nxt, double dt) {
     nxt.dT[hs] = scalar_sample(d, o, cur.dO, cur.dT, cur.tf);
     nxt.hT[hs] = scalar_sample(d, o, cur.hO, cur.hT, cur.tf);
 }
+// one thread per (axis, slot)
 __global__ void k_adv_mac(Dev d, Fields cur, Fields nxt, double dt) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.S || ghost(d, s)) return;
-    for (int a = 0; a < 3; ++a) {
-        V3 o = back_trace(d, mac_pos(d, a, s), dt, cur);
-        nxt.mac[(size_t)a * d.S + s] = comp(vel_sample(d, o, cur), a);
-    }
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 3LL * d.S) return;
+    int a = (int)(idx / d.S), s = (int)(idx - (long long)a * d.S);
+    if (ghost(d, s)) return;
+    V3 o = back_trace(d, mac_pos(d, a, s), dt, cur);
+    nxt.mac[(size_t)a * d.S + s] = comp(vel_sample(d, o, cur), a);
 }
+// one thread per (tilt, slot)
 __global__ void k_adv_tilt(Dev d, Fields cur, Fields nxt, double dt) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.S || ghost(d, s) || (nxt.tf[s] & TF_CLOSED)) return;
-    V3 c = vert_pos(d, s);
-    double e = nxt.te[s];
-    double nv[8];
-    for (int k = 0; k < 8; ++k) {
-        V3 o = back_trace(d, tilt_pos(c, k, e), dt, cur);
-        nv[k] = dot3(vel_sample(d, o, cur), tilt_up3(k));
-    }
-    for (int k = 0; k < 8; ++k) nxt.tv[(size_t)s * 8 + k] = nv[k];
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 8LL * d.S) return;
+    int s = (int)(idx >> 3), k = (int)(idx & 7);
+    if (ghost(d, s) || (nxt.tf[s] & TF_CLOSED)) return;
+    V3 o = back_trace(d, tilt_pos(vert_pos(d, s), k, nxt.te[s]), dt, cur);
+    nxt.tv[(size_t)s * 8 + k] = dot3(vel_sample(d, o, cur), tilt_up3(k));
 }
+// one thread per (half tilt, slot); unused slots are zero
 __global__ void k_adv_half(Dev d, Fields cur, Fields nxt, double dt) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.H) return;
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 8LL * d.H) return;
+    int i = (int)(idx >> 3), k = (int)(idx & 7);
     int hs = d.half[i];
     int dir = tf_dir(nxt.tf[hs]);
-    double nv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    V3 c = vert_pos(d, hs);
-    for (int q = 0; q < 5; ++q) {
-        int k = HALF_SLOT[dir][q];
+    int q = -1;
+    for (int j = 0; j < 5; ++j)
+        if (HALF_SLOT[dir][j] == k) q = j;
+    double v = 0;
+    if (q >= 0) {
+        V3 c = vert_pos(d, hs);
         V3 pos = (q == 4) ? c : tilt_pos(c, k, nxt.te[hs]);
         V3 o = back_trace(d, pos, dt, cur);
         V3 dv = (q == 4) ? v3(HALF_DIR_POS[k][0], HALF_DIR_POS[k][1], HALF_DIR_POS[k][2]) : tilt_up3(k);
-        nv[k] = dot3(vel_sample(d, o, cur), dv);
+        v = dot3(vel_sample(d, o, cur), dv);
     }
-    for (int k = 0; k < 8; ++k) nxt.tv[(size_t)hs * 8 + k] = nv[k];
+    nxt.tv[(size_t)hs * 8 + k] = v;
 }
 __global__ void k_decay(Dev d, Fields F) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -650,17 +654,17 @@ __global__ void k_decay(Dev d, Fields F) {
 }
 void launch_advect_scalars(const Dev& d, const Fields& cur, const Fields& nxt, const uint8_t* open, double dt,
                            cudaStream_t st) {
-    k_adv_scalar_oct<<<nblk(d.S), TB, 0, st>>>(d, cur, nxt, dt);
-    k_adv_scalar_tilt<<<nblk(d.S), TB, 0, st>>>(d, cur, nxt, open, dt);
-    if (d.H) k_adv_scalar_half<<<nblk(d.H), TB, 0, st>>>(d, cur, nxt, dt);
+    ASTG_LAUNCH(k_adv_scalar_oct<<<nblk(d.S), TB, 0, st>>>(d, cur, nxt, dt));
+    ASTG_LAUNCH(k_adv_scalar_tilt<<<nblk(d.S), TB, 0, st>>>(d, cur, nxt, open, dt));
+    if (d.H) ASTG_LAUNCH(k_adv_scalar_half<<<nblk(d.H), TB, 0, st>>>(d, cur, nxt, dt));
     launch_scalar_ghost(d, nxt.dO, nxt.dT, nxt.te, nxt.tf, st);
     launch_scalar_ghost(d, nxt.hO, nxt.hT, nxt.te, nxt.tf, st);
 }
 void launch_advect_velocity(const Dev& d, const Fields& cur, const Fields& nxt, double dt, cudaStream_t st) {
-    k_adv_mac<<<nblk(d.S), TB, 0, st>>>(d, cur, nxt, dt);
-    k_adv_tilt<<<nblk(d.S), TB, 0, st>>>(d, cur, nxt, dt);
-    if (d.H) k_adv_half<<<nblk(d.H), TB, 0, st>>>(d, cur, nxt, dt);
+    ASTG_LAUNCH(k_adv_mac<<<nblk(3LL * d.S), TB, 0, st>>>(d, cur, nxt, dt));
+    ASTG_LAUNCH(k_adv_tilt<<<nblk(8LL * d.S), TB, 0, st>>>(d, cur, nxt, dt));
+    if (d.H) ASTG_LAUNCH(k_adv_half<<<nblk(8LL * d.H), TB, 0, st>>>(d, cur, nxt, dt));
 }
-void launch_decay(const Dev& d, const Fields& F, cudaStream_t st) { k_decay<<<nblk(d.S), TB, 0, st>>>(d, F); }
+void launch_decay(const Dev& d, const Fields& F, cudaStream_t st) { ASTG_LAUNCH(k_decay<<<nblk(d.S), TB, 0, st>>>(d, F)); }
 
 }  // namespace astg

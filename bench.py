@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 octree smoke step.
+
+One "step" is one OctreeOmniGridSolver3 time step (source, buoyancy, projection with MIC(0)-PCG
+to relative residual 1e-6, dual velocity, tilt adaptivity, RK2 semi-Lagrangian advection) of the
+benchmark scene on the 256^3-equivalent octree (64^3 coarsest cells, 2 refinement levels), with
+synthetic inputs (seeded curl-noise velocity, sphere source).  The state (~0.3 GB) is larger than
+the 129 MB L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  Under torchrun each rank runs an independent replica on its own GPU (the
+step does not shard: MIC(0) sweeps are globally ordered); value = all ranks' steps / max time.
+The reference arm times the CPU restatement of the reference algorithm (oracle/, OpenMP over the
+host cores, bit-identical results) on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "ast-grid_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+COARSEST, LEVELS, DT = 64, 3, 0.01
+WORKLOAD = "octree smoke step, 64^3 coarsest x 3 levels (256^3-equivalent), FP64 MIC(0)-PCG to rel. residual 1e-6"
+METRIC = "smoke steps/s"
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Host-side barrier and max over ranks (gloo); no collective touches the step's data."""
+
+    def __init__(self, ws):
+        self.ws = ws
+        if ws > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, v):
+        if self.ws == 1:
+            return v
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if self.ws == 1:
+            return v
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for ln in open(self.path):
+                f = [x.strip() for x in ln.split(",")]
+                if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                    rows.append(f)
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """Per-row DRAM bytes of the dominant kernel from the committed ncu summary (or None)."""
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
+    out = {}
+    try:
+        for ln in open(path):
+            if ":" in ln and not ln.lstrip().startswith("#"):
+                k, v = ln.split(":", 1)
+                try:
+                    out[k.strip()] = float(v.split()[0])
+                except (ValueError, IndexError):
+                    pass
+    except OSError:
+        pass
+    return out
+
+
+def cpu_baseline_sample(steps):
+    """The CPU restatement of the reference's step (oracle, OpenMP) on the same workload."""
+    from oracle.oracle import Oracle
+
+    o = Oracle(COARSEST, LEVELS, openmp=True)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.step(DT)
+    el = time.perf_counter() - t0
+    o.close()
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": steps / el, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} steps of the same scene from t=0 (oracle/smoke_oracle.cpp, OpenMP, "
+                      f"bit-identical to the reference's CPU algorithm), {el:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if ws > 1 and rank != 0:
+        return 0
+    from oracle.oracle import Oracle
+
+    o = Oracle(COARSEST, LEVELS, openmp=True)
+    for _ in range(args.warmup):
+        o.step(DT)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step(DT)
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "coarsest": COARSEST, "levels": LEVELS, "dt": DT,
+                       "l2": "state larger than L2"},
+            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": f"steps {args.warmup + 1}..{args.warmup + args.steps} of the scene on the host "
+                                       f"cores (oracle/smoke_oracle.cpp, OpenMP)"},
+            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import ast_solver
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    D = Dist(ws)
+    s = ast_solver.OctreeSmoke3(COARSEST, LEVELS, device=local)
+    S = s.slots
+    for _ in range(args.warmup):
+        s.update(DT)
+    torch.cuda.synchronize()
+    D.barrier()
+
+    # ---------------- device-resident timed region
+    s.set_profiling(True)
+    l0 = s.launches
+    dev_ms = []
+    iters = []
+    pcg_ms = []
+    dofs = []
+    nnzs = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        D.barrier()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.update(DT)
+            st = s.last_step
+            dev_ms.append(st.ms_total)
+            iters.append(st.solve.iterations)
+            pcg_ms.append(st.solve.ms)
+            dofs.append(st.solve.n)
+            nnzs.append(st.solve.nnz)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+    clocks = clk.summary()
+    launches = s.launches - l0
+    kms = s.kernel_ms()
+    s.set_profiling(False)
+    t_dev = sum(dev_ms) / 1e3
+    t_max = D.max(max(t_dev, 1e-9))
+    total_steps = D.sum(args.steps)
+    value = total_steps / t_max
+
+    # ---------------- end to end through the C ABI with pinned host buffers
+    names_sync = ["density_oct", "density_tilt", "heat_oct", "heat_tilt"]
+    host = {n: torch.empty(S, dtype=torch.float64, pin_memory=True) for n in names_sync}
+    out = torch.empty(S, dtype=torch.float64, pin_memory=True)
+    lib = ast_solver.lib()
+    h2d = 8 * S * len(names_sync)
+    d2h = 8 * S * len(names_sync) + 8 * S
+
+    def e2e_step():
+        # state to the host before the scene callback and back after it (the drop-in contract of
+        # sceneSetup), one step, then the frame's density to the host
+        for n in names_sync:
+            s._check(lib.astg_get(s._h, n.encode(), host[n].data_ptr(), 8 * S, None))
+        for n in names_sync:
+            s._check(lib.astg_set(s._h, n.encode(), host[n].data_ptr(), 8 * S))
+        s.update(DT)
+        s._check(lib.astg_get(s._h, b"density_oct", out.data_ptr(), 8 * S, None))
+
+    e2e_steps = max(1, min(args.steps, 10))
+    torch.cuda.synchronize()
+    D.barrier()
+    e0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e_el = D.max(time.perf_counter() - e0)
+    e2e = {"value": D.sum(e2e_steps) / e_el, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "steps": e2e_steps}
+
+    # ---------------- roofline of the dominant kernel
+    peak, peak_kind = measured_peaks()
+    names = {"sweep_fwd": "k_sweep_fwd", "sweep_bwd": "k_sweep_bwd", "spmv_dot": "k_spmv_dot",
+             "mic_factor": "k_mic_factor"}
+    top = max(kms, key=lambda k: kms[k][0])
+    n_mean = float(np.mean(dofs))
+    nnz_mean = float(np.mean(nnzs))
+    nnzL = (nnz_mean - n_mean) / 2
+    alg = {"sweep_fwd": 12 * nnzL + 28 * n_mean, "sweep_bwd": 12 * nnzL + 28 * n_mean,
+           "spmv_dot": 12 * nnz_mean + 4 * (n_mean + 1) + 16 * n_mean + 16 * n_mean,
+           "mic_factor": 12 * nnz_mean + 12 * nnzL}[top]
+    avg_ms = kms[top][0] / max(kms[top][1], 1)
+    achieved = alg / (avg_ms / 1e3) / 1e9
+    tr = committed_traffic()
+    traffic = None
+    if f"{names[top]}_bytes_per_row" in tr:
+        traffic = tr[f"{names[top]}_bytes_per_row"] * n_mean
+    roofline = {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms, "launches": kms[top][1],
+                "note": "MIC(0) sweeps are bounded by the dependency chain (wavefront latency), not HBM"}
+    kernel_breakdown = {names[k]: {"ms_total": v[0], "launches": v[1]} for k, v in kms.items()}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(args.cpu_steps)
+
+    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "coarsest": COARSEST, "levels": LEVELS, "dt": DT,
+                       "dofs_mean": n_mean, "nnz_mean": nnz_mean, "slots": S, "precision": "fp64",
+                       "l2": "state larger than L2 (no flush)", "parallelism": f"replicas x{ws}"},
+            "pcg_ms_per_solve": float(np.mean(pcg_ms)), "pcg_iters_mean": float(np.mean(iters)),
+            "wall_ms_per_step": 1e3 * wall / args.steps,
+            "roofline": roofline, "kernels": kernel_breakdown, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": clocks, "gpu_launches": launches}
+    s.close()
+    D.barrier()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    D.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -102,11 +102,16 @@ astg_status astg_stage(astg_handle* h, int stage, double dt);
 astg_status astg_set_solver_parameters(astg_handle* h, double tol, int max_iter, double omega, double min_diag);
 astg_status astg_set_precision(astg_handle* h, astg_precision prec);
 
+/* CUDA-event timing of the PCG's main kernels (forward and backward MIC(0) sweeps, SpMV + dot,
+ * factorisation), read back as astg_get(h, "kernel_ms", ...).  No counterpart in the reference:
+ * it replaces the BENCHMARK_SCOPED_TIMER_SECTION probes (include/global_benchmark.h:33-43). */
+astg_status astg_set_profiling(astg_handle* h, int on);
+
 /* Statistics of the last projection. */
 astg_status astg_last_solve(const astg_handle* h, astg_solve_stats* out);
 
 /* Sizes: 0 slots, 1 levels, 2 finest resolution, 3 DOFs of the last projection,
- * 4 half tilts, 5 non-zeros of the last matrix. */
+ * 4 half tilts, 5 non-zeros of the last matrix, 6 kernels launched by the library so far. */
 long long astg_size(const astg_handle* h, int what);
 
 /* Copy a state array out of / into the handle.  Names (element type):

@@ -14,6 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
+LIB_OMP = os.path.join(BUILD, "liboracle_omp.so")  # same code, independent per-node loops on OpenMP threads
 SRC = os.path.join(HERE, "smoke_oracle.cpp")
 SCENE = os.path.join(ROOT, "ast-grid_gb300", "csrc")
 
@@ -29,16 +30,20 @@ SHAPES = {"mac": (3, -1), "tilt_vel": (-1, 8), "dual_oct": (-1, 3), "dual_tilt":
           "dual_tables": (128, 3, 7)}
 
 
-def build(force=False):
-    """Compile the oracle with g++ (IEEE order: no fast-math, no FP contraction)."""
+def build(force=False, openmp=False):
+    """Compile the oracle with g++ (IEEE order: no fast-math, no FP contraction).  The OpenMP
+    variant runs the reference's parallel per-node loops on threads; its results are identical."""
     os.makedirs(BUILD, exist_ok=True)
+    out = LIB_OMP if openmp else LIB
     deps = [SRC, os.path.join(SCENE, "scene.h")]
-    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
-        return LIB
-    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", SCENE, SRC, "-o", LIB + ".tmp"]
+    if not force and os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+        return out
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", SCENE, SRC, "-o", out + ".tmp"]
+    if openmp:
+        cmd.insert(1, "-fopenmp")
     subprocess.check_call(cmd)
-    os.replace(LIB + ".tmp", LIB)
-    return LIB
+    os.replace(out + ".tmp", out)
+    return out
 
 
 class _Params(ctypes.Structure):
@@ -50,13 +55,12 @@ class _Params(ctypes.Structure):
                 ("ref_workers", ctypes.c_int)]
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        _lib = ctypes.CDLL(build())
+def lib(openmp=False):
+    if openmp not in _libs:
+        _lib = ctypes.CDLL(build(openmp=openmp))
         _lib.orc_create.restype = ctypes.c_void_p
         _lib.orc_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(_Params), ctypes.c_char_p, ctypes.c_int]
         _lib.orc_destroy.argtypes = [ctypes.c_void_p]
@@ -66,7 +70,10 @@ def lib():
         _lib.orc_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_longlong]
         _lib.orc_set.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_longlong]
         _lib.orc_size.argtypes = [ctypes.c_void_p, ctypes.c_int]
-    return _lib
+        _lib.orc_solve.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 5 + [ctypes.c_double,
+                                                                                               ctypes.c_int]
+        _libs[openmp] = _lib
+    return _libs[openmp]
 
 
 class Oracle:
@@ -74,19 +81,20 @@ class Oracle:
 
     def __init__(self, coarsest, levels, tol=1e-6, buoy_d=-0.1, buoy_t=1.0, decay=1.0, rho=2.0, noise=1e-3,
                  source=(0.5, 0.5, 0.12, 0.06), seed=0, max_iter=3000, tilt_adaptivity=True, closed_mask=47,
-                 reduce_mode=0, ref_workers=8):
+                 reduce_mode=0, ref_workers=8, openmp=False):
         """reduce_mode 0 follows the reference's own reduction order (Eigen's dot, per-worker
         partial sums over ref_workers workers); 1 follows the CUDA library's fixed tree."""
         p = _Params(tol, buoy_d, buoy_t, decay, rho, noise, source[0], source[1], source[2], source[3], seed,
                     max_iter, 1 if tilt_adaptivity else 0, closed_mask, reduce_mode, ref_workers)
+        self._lib = lib(openmp)
         err = ctypes.create_string_buffer(512)
-        self._h = lib().orc_create(coarsest, levels, ctypes.byref(p), err, 512)
+        self._h = self._lib.orc_create(coarsest, levels, ctypes.byref(p), err, 512)
         if not self._h:
             raise RuntimeError("oracle: " + err.value.decode())
 
     def close(self):
         if self._h:
-            lib().orc_destroy(self._h)
+            self._lib.orc_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -98,19 +106,19 @@ class Oracle:
 
     def stage(self, i, dt):
         err = ctypes.create_string_buffer(512)
-        self._check(lib().orc_stage(self._h, i, dt, err, 512), err)
+        self._check(self._lib.orc_stage(self._h, i, dt, err, 512), err)
 
     def step(self, dt):
         err = ctypes.create_string_buffer(512)
-        self._check(lib().orc_step(self._h, dt, err, 512), err)
+        self._check(self._lib.orc_step(self._h, dt, err, 512), err)
 
     def get(self, name):
-        n = lib().orc_get(self._h, name.encode(), None, 0)
+        n = self._lib.orc_get(self._h, name.encode(), None, 0)
         if n < 0:
             raise KeyError(name)
         dt = np.float64 if name in F64 else np.int32 if name in I32 else np.int64 if name in I64 else np.uint8
         out = np.empty(n, dtype=dt)
-        lib().orc_get(self._h, name.encode(), out.ctypes.data, n)
+        self._lib.orc_get(self._h, name.encode(), out.ctypes.data, n)
         if name in SHAPES:
             out = out.reshape(SHAPES[name])
         return out
@@ -121,14 +129,25 @@ class Oracle:
         base = name[2:] if name.startswith("t_") and name[2:] in fields else name
         dt = np.int32 if base == "tilt_flags" else np.uint8 if base == "tilt_open" else np.float64
         a = np.ascontiguousarray(arr, dtype=dt).ravel()
-        rc = lib().orc_set(self._h, name.encode(), a.ctypes.data, a.size)
+        rc = self._lib.orc_set(self._h, name.encode(), a.ctypes.data, a.size)
         if rc != 0:
             raise ValueError(f"oracle: cannot set {name} ({rc})")
 
+    def solve(self, rowptr, col, val, b, tol=1e-6, max_iter=3000):
+        """PCGSolver::solve on a CSR system; returns (x, iterations)."""
+        rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+        c = np.ascontiguousarray(col, dtype=np.int32)
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(len(bb))
+        it = self._lib.orc_solve(self._h, len(bb), rp.ctypes.data, c.ctypes.data, v.ctypes.data, bb.ctypes.data,
+                                 x.ctypes.data, tol, max_iter)
+        return x, it
+
     @property
     def slots(self):
-        return lib().orc_size(self._h, 0)
+        return self._lib.orc_size(self._h, 0)
 
     @property
     def ndof(self):
-        return lib().orc_size(self._h, 3)
+        return self._lib.orc_size(self._h, 3)

@@ -343,7 +343,11 @@ public:
     }
     bool isGhostNode(int l, int x, int y, int z) {  // layout->node(...).flag & IS_GHOST
         int s = slotOf(l, x, y, z);
-        if (s < 0) { ++anomalies; return false; }
+        if (s < 0) {
+#pragma omp atomic
+            ++anomalies;
+            return false;
+        }
         return sflag[s] & F_GHOST;
     }
     double dh(int l) const { return ldh[l]; }
@@ -1212,10 +1216,12 @@ public:
         auto force = [&](V3 p) {
             return P.buoyD * scalarSample(p, dO[c], dT[c], te) + P.buoyT * (scalarSample(p, hO[c], hT[c], te) - amb);
         };
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             if (macValid(2, slev[s], sx[s], sy[s], sz[s])) mac[c][2][s] = mac[c][2][s] + dt * force(macPos(2, s));
         }
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             if (!tOpen[s]) continue;
@@ -1318,6 +1324,7 @@ public:
         const std::vector<TiltE>& te = tiltE[c];
         A.reset(nDof);
         b.assign(nDof, 0.0);
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             int ci = pO[s];
@@ -1378,6 +1385,7 @@ public:
             A.set(ci, ci, center);
             b[ci] = tb;
         }
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             int ci = pT[s];
@@ -1581,6 +1589,7 @@ public:
         s = z;
         int it;
         for (it = 0; it < P.maxIter; ++it) {
+    #pragma omp parallel for schedule(dynamic, 256)
             for (int i = 0; i < n; ++i) {
                 double t = 0;
                 for (int j = csrPtr[i]; j < csrPtr[i + 1]; ++j) t += csrVal[j] * s[csrCol[j]];
@@ -1607,6 +1616,7 @@ public:
         int c = cur;
         const std::vector<TiltE>& te = tiltE[c];
         const double k0 = dt / P.rho;
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             int l = slev[s], x = sx[s], y = sy[s], z = sz[s];
@@ -1626,6 +1636,7 @@ public:
                 mac[c][a][s] = mac[c][a][s] - k0 * (p0 - p1) / h;
             }
         }
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             if (!tOpen[s]) continue;
@@ -1689,6 +1700,7 @@ public:
         std::vector<double>& DO = dual[c][0];
         std::vector<double>& DT = dual[c][1];
         const double s3 = INV_SQRT3 * (3.0 / 4.0);
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             if (te[s].closed) { DT[3 * s] = DT[3 * s + 1] = DT[3 * s + 2] = 0; continue; }
@@ -1699,6 +1711,7 @@ public:
             for (int k = 0; k < 2; ++k) DT[3 * s + k] = ((M[k][0] * v4[0] + M[k][1] * v4[1]) + M[k][2] * v4[2]) + M[k][3] * v4[3];
             DT[3 * s + 2] = (M[2][0] * v4[0] + M[2][1] * v4[1]) + (M[2][2] * v4[2] + M[2][3] * v4[3]);
         }
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             int l = slev[s], x = sx[s], y = sy[s], z = sz[s];
@@ -1762,6 +1775,7 @@ public:
     void adjustE(double dt) {
         int c = cur, nx = 1 - cur;
         const double dTh = 0.02, vTh = EPS, maxTh = 1000;
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             if (tFixed[s]) continue;
@@ -1808,12 +1822,14 @@ public:
         int c = cur, nx = 1 - cur;
         if (P.tiltAdaptivity) adjustE(dt);
         const std::vector<TiltE>& te = tiltE[c];
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             V3 o = backTrace(cellPos(s), dt, c);
             dO[nx][s] = scalarSample(o, dO[c], dT[c], te);
             hO[nx][s] = scalarSample(o, hO[c], hT[c], te);
         }
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             if (!tOpen[s]) continue;
@@ -1831,11 +1847,13 @@ public:
         // velocity: src = buffer c, dst = buffer nx (whose tilt-E is the adjusted one)
         const std::vector<TiltE>& tn = tiltE[nx];
         for (int a = 0; a < 3; ++a)
+#pragma omp parallel for schedule(dynamic, 256)
             for (int s = 0; s < S; ++s) {
                 if (sflag[s] & F_GHOST) continue;
                 V3 o = backTrace(macPos(a, s), dt, c);
                 mac[nx][a][s] = velSample(o, c)[a];
             }
+#pragma omp parallel for schedule(dynamic, 256)
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
             if (tn[s].closed) continue;
@@ -2095,6 +2113,29 @@ int orc_set(void* h, const char* name, const void* buf, long long count) {
         return 0;
     }
     return 2;
+}
+
+// PCGSolver::solve on a caller CSR system (rows sorted by column); x receives the solution.
+// Returns the iteration count, or -1 on error.
+int orc_solve(void* h, int n, const int* rowptr, const int* col, const double* val, const double* b, double* x,
+              double tol, int max_iter) {
+    auto* s = (oracle::Solver*)h;
+    s->A.reset(n);
+    for (int i = 0; i < n; ++i)
+        for (int q = rowptr[i]; q < rowptr[i + 1]; ++q) {
+            s->A.idx[i].push_back(col[q]);
+            s->A.val[i].push_back(val[q]);
+        }
+    s->b.assign(b, b + n);
+    double saveTol = s->P.tol;
+    int saveIt = s->P.maxIter;
+    s->P.tol = tol;
+    s->P.maxIter = max_iter;
+    s->pcg();
+    s->P.tol = saveTol;
+    s->P.maxIter = saveIt;
+    memcpy(x, s->p.data(), sizeof(double) * n);
+    return s->pcgIters;
 }
 
 int orc_size(void* h, int what) {

@@ -101,3 +101,28 @@ def test_benchmark_size_bit_identical_to_oracle():
         for f in ["density_oct", "density_tilt", "heat_oct", "mac", "tilt_vel", "dual_oct", "tilt_open", "p"]:
             assert_same(f"step{k + 1}/{f}", o.get(f), s.get(f))
     s.close()
+
+
+@pytest.mark.parametrize("name", ["ref_c8_l3", "ref_c16_l2"])
+def test_standalone_solve_on_reference_systems(name):
+    """astg_solve (PCGSolver::solve) on the reference's assembled systems: bit-identical to the
+    oracle with the library's reduction tree, and within the solver tolerance of the reference."""
+    g = golden(name)
+    c, lv, steps = case(name)
+    s = solver(c, lv)
+    o = oracle(c, lv)
+    for k in range(1, steps + 1):
+        st = state(g, f"step{k}/")
+        x, stats = s.solve(st["A_rowptr"], st["A_col"], st["A_val"], st["b"])
+        xo, ito = o.solve(st["A_rowptr"], st["A_col"], st["A_val"], st["b"])
+        assert stats.converged == 1 and stats.iterations == ito
+        assert_same(f"step{k}/p vs oracle", xo, x)
+        assert abs(stats.iterations - int(st["pcg_iters"][0])) <= 1
+        assert max_rel(st["p"], x) <= 1e-6
+        # the residual test of the reference: |b - A x|_inf <= tol |b|_inf
+        rp, col, val = st["A_rowptr"], st["A_col"], st["A_val"]
+        ax = np.zeros_like(x)
+        for i in range(len(x)):
+            ax[i] = np.dot(val[rp[i]:rp[i + 1]], x[col[rp[i]:rp[i + 1]]])
+        assert np.abs(st["b"] - ax).max() <= 1e-6 * np.abs(st["b"]).max() * 1.0000001
+    s.close()

@@ -73,3 +73,16 @@ def test_tree_reduction_mode_matches_reference_order_closely():
     for f in ["density_oct", "heat_oct", "mac", "tilt_vel"]:
         ref = st[f]
         assert np.abs(o.get(f) - ref).max() <= 1e-6 * max(np.abs(ref).max(), 1e-30), f
+
+
+@pytest.mark.parametrize("name", ["ref_c8_l3", "ref_c16_l2"])
+def test_standalone_pcg_reproduces_reference_solution(name):
+    """PCGSolver::solve on the reference's own assembled system: same iterates, bit for bit."""
+    g = golden(name)
+    c, lv, steps = case(name)
+    o = Oracle(c, lv)
+    for k in range(1, steps + 1):
+        st = state(g, f"step{k}/")
+        x, it = o.solve(st["A_rowptr"], st["A_col"], st["A_val"], st["b"])
+        assert it == int(st["pcg_iters"][0])
+        assert_same(f"step{k}/p", st["p"], x)
