@@ -111,7 +111,10 @@ astg_status astg_set_profiling(astg_handle* h, int on);
 astg_status astg_last_solve(const astg_handle* h, astg_solve_stats* out);
 
 /* Sizes: 0 slots, 1 levels, 2 finest resolution, 3 DOFs of the last projection,
- * 4 half tilts, 5 non-zeros of the last matrix, 6 kernels launched by the library so far. */
+ * 4 half tilts, 5 non-zeros of the last matrix, 6 kernels launched by the library so far,
+ * 7 form of the MIC(0) preconditioner: 100 + cluster size when both sweeps run fused in one
+ * cluster launch, the cluster size of the global-memory cluster sweeps, or 0 for the sync-free
+ * sweeps. */
 long long astg_size(const astg_handle* h, int what);
 
 /* Copy a state array out of / into the handle.  Names (element type):
@@ -136,8 +139,9 @@ astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32
                        const double* b, double* x, double rel_tol, int max_iter, astg_precision prec,
                        astg_solve_stats* stats);
 
-/* Maximum |MAC velocity| over all faces, the quantity OctreeOmniGridSolver3::cfl divides by
- * the finest spacing (src/octree_omnigrid_solver3.cpp:1066-1122). */
+/* Largest MAC face value over all faces, starting from 0 (signed, as the reference's max(v)),
+ * the quantity OctreeOmniGridSolver3::cfl divides by the finest spacing
+ * (src/octree_omnigrid_solver3.cpp:1066-1122). */
 astg_status astg_max_velocity(astg_handle* h, double* out);
 
 #ifdef __cplusplus

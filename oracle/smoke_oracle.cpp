@@ -1,6 +1,6 @@
 // ORACLE — test infrastructure only.
 //
-// A plain, single-threaded C++ restatement of the reference's octree smoke step
+// A plain C++ restatement of the reference's octree smoke step
 // (YuweiXiao/AST-Grid, OctreeOmniGridSolver3).  It is the checker for the CUDA library: the
 // tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it; the library never
 // does.  Each function cites the reference file:line it restates.  It is pinned against the
@@ -20,7 +20,9 @@
 // "outside the solid" and the cut-cell weights are the constants that
 // initCuttingCellWeights (src/octree_omnigrid_solver3.cpp:1169-1238) produces for it.
 //
-// Built with FP contraction off so the arithmetic follows the reference's IEEE order.
+// Built with FP contraction off so the arithmetic follows the reference's IEEE order.  The
+// optional OpenMP build parallelises only loops whose iterations are independent (one slot or one
+// row each), so its results are bit-identical to the serial build.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
