@@ -22,7 +22,7 @@ FP64, MIXED = 0, 1
 # exported symbols of include/astg.h
 SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_stage",
            "astg_set_solver_parameters", "astg_set_precision", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
-           "astg_solve", "astg_max_velocity"]
+           "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc"]
 
 
 class AstgError(RuntimeError):
@@ -82,6 +82,8 @@ def lib(path=None):
         L.astg_solve.argtypes = [c_p, ctypes.c_int, c_p, c_p, c_p, c_p, c_p, ctypes.c_double, ctypes.c_int,
                                  ctypes.c_int, ctypes.POINTER(SolveStats)]
         L.astg_max_velocity.argtypes = [c_p, ctypes.POINTER(ctypes.c_double)]
+        L.astg_mean_temperature_noalloc.argtypes = [c_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int, c_p, c_p,
+                                                    ctypes.c_char_p, ctypes.c_size_t]
         _lib = L
     return _lib
 
@@ -246,3 +248,15 @@ class OctreeSmoke3:
         v = ctypes.c_double()
         self._check(lib().astg_max_velocity(self._h, ctypes.byref(v)))
         return v.value
+
+
+def mean_temperature_noalloc(d_heat_oct, level_slots, d_amb, stream=0):
+    """astg_mean_temperature_noalloc: ambT of the heat at device address ``d_heat_oct`` into the
+    double at device address ``d_amb``, queued on ``stream`` (a cudaStream_t as an int), with no
+    allocation; ``level_slots`` gives the slots (cells + ghosts) of each level."""
+    slots = np.ascontiguousarray(level_slots, dtype=np.int64)
+    err = ctypes.create_string_buffer(256)
+    st = lib().astg_mean_temperature_noalloc(d_heat_oct, slots.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                             len(slots), d_amb, stream or None, err, len(err))
+    if st != ASTG_OK:
+        raise AstgError(st, err.value.decode())

@@ -5,6 +5,7 @@
 // PCG's stopping test and the status word, reads a few bytes back.
 #include <algorithm>
 #include <cmath>
+#include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -992,6 +993,16 @@ astg_status guard(astg_handle* h, F&& f) {
         return fail(h, e, ASTG_CUDA_ERROR);
     }
 }
+// message of a handle-less call into the caller's buffer (which may be NULL)
+astg_status noalloc_fail(char* err, size_t errlen, astg_status s, const char* fmt, ...) {
+    if (err && errlen) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(err, errlen, fmt, ap);
+        va_end(ap);
+    }
+    return s;
+}
 }  // namespace
 
 extern "C" {
@@ -1129,6 +1140,58 @@ astg_status astg_max_velocity(astg_handle* h, double* out) {
         for (double v : mac) m = std::max(m, v);
         *out = m;
     });
+}
+
+// Takes no handle and allocates nothing, on the device or the host: the chunk partials go to a
+// static device array (launch_mean_temperature_static), so callers that must not allocate can
+// use it.  Which callers those are, and the rules on the shared array, are in include/astg.h.
+astg_status astg_mean_temperature_noalloc(const double* d_heat_oct, const int64_t* level_slots, int levels,
+                                          double* d_amb, void* stream, char* err, size_t errlen) {
+    if (err && errlen) err[0] = 0;
+    if (!d_heat_oct || !d_amb || !level_slots) return noalloc_fail(err, errlen, ASTG_BAD_ARG, "null pointer argument");
+    if (levels < 1 || levels > MAXL)
+        return noalloc_fail(err, errlen, ASTG_BAD_ARG, "levels = %d, must be 1..%d", levels, MAXL);
+    LevelSpans sp;
+    sp.L = levels;
+    sp.off[0] = 0;
+    sp.partOff[0] = 0;
+    for (int l = 0; l < levels; ++l) {
+        long long n = level_slots[l];
+        if (n < 0) return noalloc_fail(err, errlen, ASTG_BAD_ARG, "level %d has a negative slot count %lld", l, n);
+        long long m = (n + AMB_CHUNK - 1) / AMB_CHUNK;
+        if (m > AMB_MAX_LEVEL_PARTIALS)
+            return noalloc_fail(err, errlen, ASTG_BAD_ARG, "level %d has %lld slots, more than %d * %d", l, n,
+                                AMB_CHUNK, AMB_MAX_LEVEL_PARTIALS);
+        sp.off[l + 1] = sp.off[l] + n;
+        if (sp.partOff[l] + m > NOALLOC_MAX_PARTIALS)
+            return noalloc_fail(err, errlen, ASTG_BAD_ARG,
+                                "%lld slots need more than the %d partials of the static scratch "
+                                "(sum over levels of ceil(slots / %d) must be <= %d)",
+                                sp.off[l + 1], NOALLOC_MAX_PARTIALS, AMB_CHUNK, NOALLOC_MAX_PARTIALS);
+        sp.partOff[l + 1] = sp.partOff[l] + (int)m;
+    }
+    if (sp.off[levels] == 0) return noalloc_fail(err, errlen, ASTG_BAD_ARG, "no slots");
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return noalloc_fail(err, errlen, ASTG_NO_DEVICE, "no CUDA device");
+    }
+    const void* ptrs[2] = {d_heat_oct, d_amb};
+    const char* names[2] = {"d_heat_oct", "d_amb"};
+    for (int k = 0; k < 2; ++k) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, ptrs[k]) != cudaSuccess) {
+            cudaGetLastError();
+            return noalloc_fail(err, errlen, ASTG_BAD_ARG, "%s is not a CUDA pointer", names[k]);
+        }
+        bool onDevice = a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+        if (!onDevice || (a.type == cudaMemoryTypeDevice && a.device != dev))
+            return noalloc_fail(err, errlen, ASTG_BAD_ARG, "%s is not device memory of the current device %d",
+                                names[k], dev);
+    }
+    cudaError_t e = launch_mean_temperature_static(d_heat_oct, sp, d_amb, (cudaStream_t)stream);
+    if (e != cudaSuccess) return noalloc_fail(err, errlen, ASTG_CUDA_ERROR, "CUDA error: %s", cudaGetErrorString(e));
+    return ASTG_OK;
 }
 
 }  // extern "C"

@@ -107,6 +107,17 @@ void launch_scalar_ghost(const Dev& d, double* oct, double* til, const double* t
 void launch_dual_ghost(const Dev& d, const Fields& F, cudaStream_t st);
 void launch_mean_temperature(const Dev& d, const double* hO, double* parts, const int* partOffDev,
                              const int* partOffHost, double* amb, cudaStream_t st);
+// mean temperature over a caller's device array with its scratch in a static device array
+constexpr int AMB_CHUNK = 2048;                 // elements per partial of the fixed reduction tree
+constexpr int AMB_MAX_LEVEL_PARTIALS = 2048;    // partials of one level folded by one block
+constexpr int NOALLOC_MAX_PARTIALS = 8192;      // 64 KiB of static scratch per device
+constexpr int NOALLOC_MAX_DEVICES = 64;
+struct LevelSpans {
+    int L;
+    long long off[MAXL + 1];  // first slot of each level; off[L] = all slots
+    int partOff[MAXL + 1];    // first partial of each level
+};
+cudaError_t launch_mean_temperature_static(const double* heat, const LevelSpans& sp, double* amb, cudaStream_t st);
 void launch_force(const Dev& d, const Fields& F, const uint8_t* open, const double* amb, double dt, cudaStream_t st);
 void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);
 void launch_dof_numbering(const Dev& d, const uint8_t* open, Proj& P, cudaStream_t st);

@@ -15,6 +15,7 @@
 #include <cooperative_groups.h>
 #include <cstdio>
 #include <cstdlib>
+#include <mutex>
 
 #include "astg_launch.h"
 #include "astg_sample.cuh"
@@ -132,6 +133,77 @@ void launch_mean_temperature(const Dev& d, const double* hO, double* parts, cons
         if (m > 0) ASTG_LAUNCH(k_tree_sum<<<m, RED_LANES, 0, st>>>(hO + d.loff[l], nullptr, n, parts + partOffHost[l]));
     }
     ASTG_LAUNCH(k_amb<<<1, RED_LANES, 0, st>>>(d, parts, partOffDev, amb));
+}
+
+// ------------------------------------------------------------------ mean temperature, static scratch
+// The same reduction for callers that hold the heat array in their own device memory and must not
+// allocate: a framework whose caching allocator has already reserved most of HBM (a cudaMalloc
+// there can fail or force the framework to release its cache), or a per-step loop on a shared
+// device that cannot take the device-wide synchronisation cudaMalloc and cudaFree imply.  The chunk
+// partials live in one file-scope device array instead of handle memory.  Each call writes every
+// partial it later reads, on the same stream, so nothing in the array has to start at zero.  All
+// calls on one device share the array: two calls whose kernels overlap in time (different streams,
+// or different host threads without ordering between them) race on it.
+static_assert(RED_CHUNK == AMB_CHUNK, "one chunk size for both forms of the reduction");
+static __device__ __align__(256) double g_amb_scratch[NOALLOC_MAX_PARTIALS];
+
+// one block per chunk of any level: the arithmetic of k_tree_sum on that level's slice
+__global__ void k_tree_sum_levels(const double* a, LevelSpans sp, double* part) {
+    __shared__ double sh[RED_LANES];
+    int b = blockIdx.x, l = 0;
+    while (l + 1 < sp.L && b >= sp.partOff[l + 1]) ++l;
+    long long n = sp.off[l + 1] - sp.off[l];
+    long long base = (long long)(b - sp.partOff[l]) * RED_CHUNK;
+    const double* al = a + sp.off[l];
+    double acc = 0.0;
+    for (int k = 0; k < RED_PER_LANE; ++k) {
+        long long i = base + threadIdx.x + (long long)RED_LANES * k;
+        if (i < n) acc = acc + al[i];
+    }
+    double r = block_tree(acc, sh);
+    if (threadIdx.x == 0) part[b] = r;
+}
+// the arithmetic of k_amb with the level bounds passed by value
+__global__ void k_amb_levels(LevelSpans sp, const double* parts, double* amb) {
+    __shared__ double sh[RED_LANES];
+    double total = 0.0;
+    long long count = 0;
+    for (int l = 0; l < sp.L; ++l) {
+        long long m = sp.partOff[l + 1] - sp.partOff[l];
+        double s = m > 0 ? fold_partials(parts + sp.partOff[l], m, sh) : 0.0;
+        total += s * (l == 0 ? 1 : 8);
+        count += (sp.off[l + 1] - sp.off[l]) * (l == 0 ? 1 : 8);
+    }
+    if (threadIdx.x == 0) *amb = total / (double)count;
+}
+
+// Address of g_amb_scratch on the current device, looked up on the first call made with each
+// device current and kept; the lookup may load this library's device code on that device.
+static std::mutex g_amb_scratch_mu;
+static double* g_amb_scratch_ptr[NOALLOC_MAX_DEVICES];
+cudaError_t mean_temperature_scratch(double** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_amb_scratch_mu);
+    if (!g_amb_scratch_ptr[dev]) {
+        double* p = nullptr;
+        e = cudaGetSymbolAddress((void**)&p, g_amb_scratch);
+        if (e != cudaSuccess) return e;
+        g_amb_scratch_ptr[dev] = p;
+    }
+    *out = g_amb_scratch_ptr[dev];
+    return cudaSuccess;
+}
+cudaError_t launch_mean_temperature_static(const double* heat, const LevelSpans& sp, double* amb, cudaStream_t st) {
+    double* parts = nullptr;
+    cudaError_t e = mean_temperature_scratch(&parts);
+    if (e != cudaSuccess) return e;
+    int m = sp.partOff[sp.L];
+    if (m > 0) ASTG_LAUNCH(k_tree_sum_levels<<<m, RED_LANES, 0, st>>>(heat, sp, parts));
+    ASTG_LAUNCH(k_amb_levels<<<1, RED_LANES, 0, st>>>(sp, parts, amb));
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ exclusive scan (int)

@@ -144,6 +144,33 @@ astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32
  * (src/octree_omnigrid_solver3.cpp:1066-1122). */
 astg_status astg_max_velocity(astg_handle* h, double* out);
 
+/* Mean temperature ambT of addForce (src/octree_omnigrid_solver3.cpp:922-929) over an octagon heat
+ * array the caller keeps in its own device memory.  It is the reduction astg_step runs in its force
+ * stage, with the same fixed summation tree, so the result equals astg_get(h, "ambT") bit for bit
+ * for the same heat.  No counterpart in the reference: it exists for callers that must not
+ * allocate, such as a framework whose caching allocator has reserved most of the device's memory,
+ * or a per-step loop on a shared device that cannot take the device-wide synchronisation of
+ * cudaMalloc / cudaFree.  It takes no handle and allocates nothing: its scratch (the chunk partials)
+ * is one static 64 KiB device array per device.
+ *   d_heat_oct   device pointer: the heat of all levels in "heat_oct" order (level-major, then the
+ *                reference's layout index, ghosts included)
+ *   level_slots  host array of `levels` counts: slots (cells + ghosts) per level, column 2 of
+ *                astg_get(h, "level_sizes")
+ *   d_amb        device pointer receiving one double
+ *   stream       the cudaStream_t to run on (NULL: the legacy default stream); the call returns once
+ *                the work is queued, and d_amb is valid when the stream reaches it
+ *   err, errlen  optional buffer for the reason of a failed call
+ * Limits: 1 <= levels <= 6; at most 2048 * 2048 slots per level; the sum over levels of
+ * ceil(slots / 2048) at most 8192.  Larger inputs return ASTG_BAD_ARG and say which limit failed.
+ * Nothing in the scratch needs to start at zero: each call writes every partial it reads.
+ * The first call with each device current looks up the scratch's address (cudaGetSymbolAddress),
+ * which may load this library's device code onto that device; make that first call before any
+ * stream capture begins.  All calls on one device share the scratch: calls whose kernels may
+ * overlap in time (different streams, or host threads without ordering between them) race on it
+ * and must be serialised by the caller. */
+astg_status astg_mean_temperature_noalloc(const double* d_heat_oct, const int64_t* level_slots, int levels,
+                                          double* d_amb, void* stream, char* err, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif
