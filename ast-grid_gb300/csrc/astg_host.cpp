@@ -587,11 +587,20 @@ struct astg_handle {
         ck(cudaStreamSynchronize(st), "init");
     }
 
+    // most rows a projection can have: an octagon and a tilt DOF on every non-ghost slot, plus the
+    // half tilts
+    long long rowCapacity() const {
+        long long cells = 0;
+        for (int l = 0; l < L; ++l) cells += lN[l];
+        return 2 * cells + H;
+    }
+
     void allocProj() {
-        long long rows = (long long)S + H;
+        long long rows = rowCapacity();
+        if (rows * ROW_W >= (1LL << 31)) throw std::invalid_argument("octree too large for 32-bit matrix indices");
+        J.rowsCap = (int)rows;
         J.cnt = dalloc<int>(S);
         J.base = dalloc<int>(S);
-        J.bsum = dalloc<int>((rows + 1023) / 1024 + 1);
         J.n0 = dalloc<int>(1);
         J.nDof = dalloc<int>(1);
         J.nnz = dalloc<int>(4);  // nnz, then scan totals of the level schedule
@@ -626,12 +635,30 @@ struct astg_handle {
         J.fval = dalloc<double>(rows * ROW_W / 2 + 1);
         J.bcol = dalloc<int>(rows * ROW_W / 2 + 1);
         J.bval = dalloc<double>(rows * ROW_W / 2 + 1);
+        // MIC(0) sweep form: ASTG_SWEEP = async (default: fused, barrier-free), dsmem (fused, one
+        // cluster barrier per level), cluster (global-memory level sweeps) or syncfree (per-row
+        // flags); a form the device cannot run falls back to the next one
         const char* env = getenv("ASTG_SWEEP");
-        std::string mode = env ? env : "";
+        std::string mode = env ? env : "async";
+        if (mode != "async" && mode != "dsmem" && mode != "cluster" && mode != "syncfree")
+            throw std::invalid_argument("ASTG_SWEEP must be async, dsmem, cluster or syncfree");
         J.clusterSize = mode == "syncfree" ? 0 : choose_cluster_size(P.device);
-        J.pcCluster = (mode == "syncfree" || mode == "cluster") ? 0 : choose_dsmem_cluster((int)rows, &J.pcSmem);
-        if (J.pcCluster == 0) J.pcSmem = 0;
-        J.rowsCap = (int)rows;
+        J.pcAsync = mode == "async";
+        J.pcCluster = (mode == "async" || mode == "dsmem") ? choose_dsmem_cluster(J.pcAsync, &J.pcSmemMax) : 0;
+        J.pcActive = 0;
+        J.pcSmem = 0;
+        J.pcLgBlock = 8;  // 256-row ownership blocks (measured: 64 to 4096 within 3 %)
+        long long scanMax = std::max(rows + 1, (long long)std::max(J.pcCluster, 1) * (rows + 1));
+        J.bsum = dalloc<int>((scanMax + 1023) / 1024 + 1);
+        if (J.pcCluster && J.pcAsync) {
+            J.chunk = dalloc<int>(1);
+            J.ownStart = dalloc<int>(J.pcCluster + 1);
+            J.lself = dalloc<int>(rows);
+            J.yl = dalloc<double>(rows);
+            J.ownCnt = dalloc<int>((rows + 1) * J.pcCluster);
+            J.ownPtr = dalloc<int>((rows + 1) * J.pcCluster + 1);
+            J.ownFill = dalloc<int>((rows + 1) * J.pcCluster);
+        }
         if (J.pcCluster) {
             J.pos = dalloc<int>(rows);
             J.lcntF = dalloc<int>(rows);
@@ -675,7 +702,7 @@ struct astg_handle {
     // factorises the system held in the projection workspace and runs the PCG; J.x holds the result
     void solveCurrent(double tol, int maxIter) {
         launch_factor(d, J, P.omega, P.min_diag, epoch, st, &prof);
-        if (J.clusterSize > 0 || J.pcCluster > 0) launch_level_schedule(d, J, st);
+        if (J.clusterSize > 0 || J.pcActive) launch_level_schedule(d, J, st);
         ck(cudaEventRecord(evA, st), "event");
         launch_pcg_fp64(d, J, tol, maxIter, epoch, 8, st, &prof);
         ck(cudaEventRecord(evB, st), "event");
@@ -684,6 +711,11 @@ struct astg_handle {
     void project(double dt) {
         Fields& C = F[cur];
         launch_dof_numbering(d, dOpen, J, st);
+        int n = 0;
+        ck(cudaMemcpyAsync(&n, J.nDof, sizeof n, cudaMemcpyDeviceToHost, st), "dofs");
+        ck(cudaStreamSynchronize(st), "dofs");
+        if (n > J.rowsCap) throw std::runtime_error("projection has more rows than the workspace holds");
+        select_preconditioner(J, n);
         launch_assemble(d, C, dOpen, J, dHoPtr, dHoIdx, dt, st);
         solveCurrent(P.tol, P.max_iter);
         launch_pressure_update(d, C, dOpen, J.pO, J.pT, J.x, dt, st);
@@ -719,8 +751,9 @@ struct astg_handle {
     // workspace of the handle)
     void solveExternal(int n, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
                        double* x, double tol, int maxIter, astg_solve_stats* stats) {
-        long long rows = (long long)S + H;
-        if (n <= 0 || n > rows) throw std::invalid_argument("astg_solve: n exceeds the handle's capacity (slots + half tilts)");
+        long long rows = J.rowsCap;
+        if (n <= 0 || n > rows)
+            throw std::invalid_argument("astg_solve: n exceeds the handle's capacity (2 x cells + half tilts)");
         long long nnz = rowptr[n];
         if (nnz <= 0 || nnz > rows * ROW_W) throw std::invalid_argument("astg_solve: too many non-zeros for the workspace");
         for (int i = 0; i < n; ++i)
@@ -733,6 +766,7 @@ struct astg_handle {
         ck(cudaMemcpyAsync(J.col, col, sizeof(int) * nnz, cudaMemcpyHostToDevice, st), "upload");
         ck(cudaMemcpyAsync(J.val, val, sizeof(double) * nnz, cudaMemcpyHostToDevice, st), "upload");
         ck(cudaMemcpyAsync(J.b, b, sizeof(double) * n, cudaMemcpyHostToDevice, st), "upload");
+        select_preconditioner(J, n);
         launch_external_system(d, J, n, st);
         checkStatus();
         solveCurrent(tol, maxIter);
@@ -1102,7 +1136,7 @@ long long astg_size(const astg_handle* h, int what) {
         case 4: return h->H;
         case 5: return h->last.nnz;
         case 6: return astg::g_launches;
-        case 7: return h->J.pcCluster > 0 ? 100 + h->J.pcCluster : h->J.clusterSize;
+        case 7: return h->J.pcActive ? (h->J.pcAsync ? 200 : 100) + h->J.pcCluster : h->J.clusterSize;
         default: return -1;
     }
 }

@@ -26,8 +26,8 @@ struct KProf {
     bool created = false;
 };
 
-constexpr int ROW_W = 32;
-constexpr int PC_MAXE = 8;  // factor entries per row held in the padded records  // padded row width during assembly (rows have at most ~21 entries)
+constexpr int ROW_W = 32;   // padded row width during assembly (rows have at most ~21 entries)
+constexpr int PC_MAXE = 8;  // factor entries per row held in the padded records
 
 // scalars of the PCG kept on the device
 enum { SC_RESID0 = 0, SC_TOL, SC_RHO, SC_RESID, SC_ALPHA, SC_BETA, SC_COUNT };
@@ -76,7 +76,9 @@ struct Proj {
     int* bcol;       // nnz: level-ordered upper entries
     double* bval;
     int clusterSize; // CTAs per cluster of the level-synchronous sweeps (0: sync-free sweeps)
-    int pcCluster;   // CTAs per cluster of the fused DSMEM preconditioner (0: not used)
+    int pcCluster;   // CTAs per cluster of the fused DSMEM preconditioner (0: not available)
+    int pcActive;    // the current solve uses it (its vector fits in the cluster's shared memory)
+    size_t pcSmemMax;  // largest dynamic shared memory per CTA it may use
     // padded level-ordered records for the fused preconditioner (entry e of row p at e * rowsCap + p)
     int rowsCap;
     int* pos;        // rows: level position of each row (inverse of perm)
@@ -84,11 +86,22 @@ struct Proj {
     int* lcntB;
     double* linvd;   // rows: pivot reciprocal in level order
     double* rl;      // rows: right-hand side of the preconditioner in level order
+    // barrier-free form: row j is computed by, and stored in, CTA (j >> lgB) mod CS; each CTA walks
+    // its own rows sorted by level (positions [ownStart[c], ownStart[c + 1]))
+    int pcAsync;     // 1: barrier-free fused preconditioner, 0: one cluster barrier per level
+    int pcLgBlock;   // log2 of the rows per ownership block: row j belongs to CTA (j >> lgB) mod CS
+    int* chunk;      // device scalar: shared-memory slots per CTA
+    int* ownStart;   // CS + 1: first position of each CTA's rows
+    int* lself;      // rows: local (shared-memory) index of the row at each position
+    double* yl;      // rows: forward-sweep result at each position
+    int* ownCnt;     // pcCluster * (rows + 1): rows per (owner CTA, level)
+    int* ownPtr;
+    int* ownFill;
     int* fcolP;      // PC_MAXE * rowsCap
     double* fvalP;
     int* bcolP;
     double* bvalP;
-    size_t pcSmem;   // its dynamic shared memory per CTA
+    size_t pcSmem;   // its dynamic shared memory per CTA in the current solve
     // PCG
     double* x;
     double* r;
@@ -126,7 +139,10 @@ void launch_assemble(const Dev& d, const Fields& F, const uint8_t* open, Proj& P
 void launch_level_schedule(const Dev& d, Proj& P, cudaStream_t st);
 void launch_external_system(const Dev& d, Proj& P, int rows, cudaStream_t st);
 int choose_cluster_size(int device);
-int choose_dsmem_cluster(int maxRows, size_t* smemBytes);
+// cluster size (16 or 8) for the fused preconditioner (barrier-free form when async), or 0
+int choose_dsmem_cluster(bool async, size_t* smemMax);
+// per solve: whether the fused preconditioner holds a vector of n rows (sets pcActive, pcSmem)
+void select_preconditioner(Proj& P, int n);
 extern cudaError_t g_cluster_error;  // last failed cluster launch (cudaSuccess if none)
 void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st, KProf* prof);
 int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& epoch, int batch, cudaStream_t st,

@@ -56,6 +56,11 @@ static void prof_drain(KProf* p) {
 
 constexpr int TB = 256;
 static inline int nblk(long long n) { return (int)((n + TB - 1) / TB); }
+static int log2_exact(int v) {
+    int lg = 0;
+    while ((1 << lg) < v) ++lg;
+    return lg;
+}
 constexpr int RED_LANES = 256, RED_PER_LANE = 8, RED_CHUNK = RED_LANES * RED_PER_LANE;
 constexpr long long SPIN_LIMIT = 1LL << 24;  // ~seconds at nanosleep(64): far above any real wait
 
@@ -580,7 +585,7 @@ __global__ void k_zero_rows(Proj P, int maxRows) {
 }
 void launch_assemble(const Dev& d, const Fields& F, const uint8_t* open, Proj& P, const int* hoPtr, const int* hoIdx,
                      double dt, cudaStream_t st) {
-    int maxRows = d.S + d.H;
+    int maxRows = P.rowsCap;
     ASTG_LAUNCH(k_zero_rows<<<nblk(maxRows), TB, 0, st>>>(P, maxRows));
     ASTG_LAUNCH(k_asm_oct<<<nblk(d.S), TB, 0, st>>>(d, F, P, hoPtr, hoIdx));
     ASTG_LAUNCH(k_asm_tilt<<<nblk(d.S), TB, 0, st>>>(d, F, P, open));
@@ -913,6 +918,187 @@ __global__ void __launch_bounds__(256, 1) k_precond_dsmem(Proj P, double* z, int
     for (int j = threadIdx.x; (j << lgCS) + rank < n; j += blockDim.x) z[(j << lgCS) + rank] = zsh[j];
     cl.sync();
 }
+// ---- barrier-free fused preconditioner.  Same vector placement idea (z in the distributed
+// shared memory of one cluster), but no barrier per level: CTA c computes the rows it stores
+// (rows [c * chunk, (c + 1) * chunk)), each thread takes every blockDim-th of its CTA's rows in
+// level order, and a row waits only for the entries it reads.  An entry's readiness is its own
+// value: every slot starts as PCA_EMPTY, a signalling-NaN bit pattern that no floating-point
+// operation produces (arithmetic on NaN returns a quiet NaN), and a single aligned 8-byte store
+// makes the value visible, so no separate flag is needed.  Deadlock cannot occur: every thread
+// walks its rows in non-decreasing level order, rows read only rows of strictly lower levels
+// (forward) or higher levels (backward, walked in reverse), and all CTAs of a cluster are
+// resident together.  Every wait is bounded; on timeout the kernel records DS_WAIT_TIMEOUT, stops
+// waiting everywhere and finishes with invalid values.  Per row the operations are the
+// reference's, in the reference's order.
+constexpr int PCA_THREADS = 256;
+constexpr unsigned long long PCA_EMPTY = 0x7FF4DEADBEEF0001ull;
+constexpr long long PCA_SPIN_LIMIT = 1LL << 22;
+// Polls are plain (weak) shared-memory loads kept in place by asm volatile: shared memory is not
+// cached, so each one reads the slot's current contents, and an aligned 8-byte store is seen
+// whole or not at all.  The value itself is the signal, so nothing else needs ordering; the cluster
+// barrier at the end of each sweep orders everything for what follows.  (Loads with .relaxed.cluster
+// semantics measured about 20x slower per polling pass with every warp of the cluster polling.)
+__device__ __forceinline__ unsigned long long pca_ld_remote(uint32_t a) {
+    unsigned long long v;
+    asm volatile("ld.shared::cluster.b64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ void pca_st_local(uint32_t a, double v) {
+    asm volatile("st.shared.b64 [%0], %1;" ::"r"(a), "l"((unsigned long long)__double_as_longlong(v)) : "memory");
+}
+struct PcaRow {
+    int p, self, cnt;
+    double rhs, invd;
+    int col[PC_MAXE];
+    double val[PC_MAXE];
+};
+// record of position p (valid when q < cnt): independent loads only
+__device__ __forceinline__ void pca_load(const Proj& P, int base, int q, int rows, bool fwd, PcaRow& w) {
+    w.cnt = -1;
+    if (q < 0 || q >= rows) return;
+    const int p = base + q;
+    const int cap = P.rowsCap;
+    const int* cc = fwd ? P.fcolP : P.bcolP;
+    const double* vv = fwd ? P.fvalP : P.bvalP;
+    w.p = p;
+    w.self = P.lself[p];
+    w.cnt = fwd ? P.lcntF[p] : P.lcntB[p];
+    w.invd = P.linvd[p];
+    w.rhs = fwd ? P.rl[p] : P.yl[p];
+#pragma unroll
+    for (int e = 0; e < PC_MAXE; ++e) {
+        w.col[e] = cc[(size_t)e * cap + p];
+        w.val[e] = vv[(size_t)e * cap + p];
+    }
+}
+// One row per lane; the warp polls until every lane's row is done.  A lane consumes its entries
+// strictly in order (the reference's order) as far as they hold values, and stores its row the
+// moment the last one arrives, so no lane ever waits for a lane of its own warp while holding its
+// own result back.  The loop and its exit are warp-uniform.  Entry addresses are resolved once per
+// row into the cluster's shared-memory window (mapa), so every poll is one load form for local
+// and remote entries alike; every pass re-loads all entries still missing, so they resolve in
+// parallel.  Bounded: after PCA_SPIN_LIMIT polls (or once any wait of the launch has given up) the
+// warp stops waiting and reports.
+__device__ __forceinline__ uint32_t pca_window(uint32_t own, int packed) {
+    uint32_t a = own + (uint32_t)(packed & 0xffffff) * 8u, m;
+    asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(m) : "r"(a), "r"((uint32_t)(packed >> 24)));
+    return m;
+}
+constexpr int PCA_MAXE = 2 * PC_MAXE;  // entries a row resolves in registers (8 from the record)
+// The polling pass is integer-only: it re-loads the entries not yet known to hold values and
+// extends the prefix of present ones.  The FP64 arithmetic runs once per row, after every entry is
+// present, in the reference's order (FP64 issue is scarce on this part, and predicated-off FP64
+// instructions in a polling pass would still occupy the FP64 pipe on every pass).
+__device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaRow& w, bool fwd, uint32_t own, int* status) {
+    bool done = w.cnt < 0;
+    uint32_t a[PCA_MAXE];
+    double val[PCA_MAXE];
+#pragma unroll
+    for (int e = 0; e < PC_MAXE; ++e) {
+        a[e] = pca_window(own, w.col[e]);
+        val[e] = w.val[e];
+    }
+    // entries 8..15 of a longer row: loaded once, together, before any polling
+    const int* oc = fwd ? P.fcol : P.bcol;
+    const double* ov = fwd ? P.fval : P.bval;
+    const int q0 = (!done && w.cnt > PC_MAXE) ? (fwd ? P.fptr : P.bptr)[w.p] : 0;
+#pragma unroll
+    for (int e = PC_MAXE; e < PCA_MAXE; ++e) {
+        bool has = e < w.cnt;
+        a[e] = pca_window(own, has ? oc[q0 + e] : 0);
+        val[e] = has ? ov[q0 + e] : 0.0;
+    }
+    const int lim = min(w.cnt, PCA_MAXE);
+    unsigned long long v[PCA_MAXE];
+    int got = 0;        // leading entries known to hold values
+    bool part = false;  // the first lim entries are accumulated (rows longer than PCA_MAXE)
+    double acc = w.rhs;
+    for (long long it = 0;; ++it) {
+        if (!done) {
+            if (!part) {
+                const int g0 = got;
+#pragma unroll
+                for (int e = 0; e < PCA_MAXE; ++e)
+                    if (e >= g0 && e < lim) v[e] = pca_ld_remote(a[e]);
+#pragma unroll
+                for (int e = 0; e < PCA_MAXE; ++e)
+                    if (e == got && e < lim && v[e] != PCA_EMPTY) got = e + 1;
+                if (got == lim) {
+#pragma unroll
+                    for (int e = 0; e < PCA_MAXE; ++e) {
+                        if (e >= lim) break;
+                        acc = acc - val[e] * __longlong_as_double((long long)v[e]);
+                    }
+                    part = true;
+                }
+            }
+            // rows longer than PCA_MAXE entries: the rest one at a time from the compact arrays
+            while (part && got < w.cnt) {
+                unsigned long long x = pca_ld_remote(pca_window(own, oc[q0 + got]));
+                if (x == PCA_EMPTY) break;
+                acc = acc - ov[q0 + got] * __longlong_as_double((long long)x);
+                ++got;
+            }
+            if (part && got >= w.cnt) {
+                double y = acc * w.invd;
+                if (fwd) P.yl[w.p] = y;
+                pca_st_local(own + (uint32_t)w.self * 8u, y);
+                done = true;
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        if ((it & 255) == 255) {
+            bool over = it > PCA_SPIN_LIMIT;
+            if (over) atomicCAS(status, 0, DS_WAIT_TIMEOUT);
+            if (__any_sync(0xffffffffu, over || *(volatile int*)status != 0)) break;
+        }
+    }
+}
+__global__ void __launch_bounds__(PCA_THREADS, 1) k_precond_async(Proj P, double* z, int* status, int lgCS) {
+    if (*P.done) return;
+    extern __shared__ double zsh[];
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = cl.block_rank();
+    const int n = *P.nDof, chunk = *P.chunk;
+    const int base = P.ownStart[rank];
+    const int rows = P.ownStart[rank + 1] - base;
+    const int lgB = P.pcLgBlock;
+    const uint32_t own = (uint32_t)__cvta_generic_to_shared(zsh);
+    unsigned long long* zraw = reinterpret_cast<unsigned long long*>(zsh);
+    for (int l = threadIdx.x; l < chunk; l += blockDim.x) zraw[l] = PCA_EMPTY;
+    cl.sync();  // every CTA is running and every slot of the cluster is empty
+    for (int dir = 0; dir < 2; ++dir) {
+        const bool fwd = dir == 0;
+        // list index k of this CTA's walk -> position offset (forward: ascending levels, backward:
+        // descending)
+        auto qof = [&](int k) { return fwd ? k : rows - 1 - k; };
+        // thread t takes entries t, t + blockDim, ...: the same number of rounds for every thread,
+        // so warps stay whole; the next record is loaded while the current row waits
+        const int T = (int)blockDim.x;
+        const int rounds = (rows + T - 1) / T;
+        auto pick = [&](int k) {
+            int q = threadIdx.x + k * T;
+            return q < rows ? qof(q) : -1;
+        };
+        PcaRow W, X;
+        pca_load(P, base, pick(0), rows, fwd, W);
+        for (int k = 0; k < rounds; ++k) {
+            pca_load(P, base, pick(k + 1), rows, fwd, X);
+            pca_solve_row(P, W, fwd, own, status);
+            W = X;
+        }
+        cl.sync();  // sweep finished everywhere (global and shared writes ordered at cluster scope)
+        if (fwd) {
+            for (int l = threadIdx.x; l < chunk; l += blockDim.x) zraw[l] = PCA_EMPTY;
+            cl.sync();
+        }
+    }
+    // local slot l holds row ((l >> lgB) << lgCS | rank) << lgB | (l mod B)
+    for (int l = threadIdx.x; l < chunk; l += blockDim.x) {
+        int j = ((((l >> lgB) << lgCS) | rank) << lgB) | (l & ((1 << lgB) - 1));
+        if (j < n) z[j] = zsh[l];
+    }
+}
 static cudaError_t launch_precond_dsmem(const Proj& P, const double* r, double* z, cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(P.pcCluster);
@@ -932,34 +1118,51 @@ static cudaError_t launch_precond_dsmem(const Proj& P, const double* r, double* 
     (void)r;
     return cudaLaunchKernelEx(&cfg, k_precond_dsmem, P, z, lg);
 }
-// cluster size (16 or 8) whose distributed shared memory holds a vector of maxRows doubles, or 0
-int choose_dsmem_cluster(int maxRows, size_t* smemBytes) {
-    cudaFuncSetAttribute((const void*)k_precond_dsmem, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+static cudaError_t launch_precond_async(const Dev& d, const Proj& P, double* z, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(P.pcCluster);
+    cfg.blockDim = dim3(PCA_THREADS);
+    cfg.dynamicSmemBytes = P.pcSmem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = P.pcCluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    ++g_launches;
+    return cudaLaunchKernelEx(&cfg, k_precond_async, P, z, d.status, log2_exact(P.pcCluster));
+}
+// Cluster size (16, else 8) at which the fused preconditioner (barrier-free form when async) can
+// run with the largest dynamic shared memory a CTA may have, or 0; *smemMax = that largest size.
+// Each solve then uses ceil(n / CS) doubles per CTA and falls back to the global-memory sweeps
+// when they do not fit.
+int choose_dsmem_cluster(bool async, size_t* smemMax) {
+    const void* kern = async ? (const void*)k_precond_async : (const void*)k_precond_dsmem;
+    const int threads = async ? PCA_THREADS : PC_THREADS;
+    *smemMax = 0;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    // the attribute is process-wide: allow the device maximum once (minus the kernel's static
-    // shared memory), size each launch per handle
+    // the attribute is process-wide: allow the device maximum (minus the kernel's static shared
+    // memory) once, size each launch per solve
     cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, (const void*)k_precond_dsmem) != cudaSuccess) {
+    if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) {
         cudaGetLastError();
-        *smemBytes = 0;
         return 0;
     }
     optin -= (int)fa.sharedSizeBytes;
-    if (cudaFuncSetAttribute((const void*)k_precond_dsmem, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) !=
-        cudaSuccess) {
+    if (optin <= 0 || cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
         cudaGetLastError();
-        *smemBytes = 0;
         return 0;
     }
     for (int cs : {16, 8}) {
-        size_t bytes = (size_t)((maxRows + cs - 1) / cs) * sizeof(double);
-        if (bytes > (size_t)optin) continue;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cs);
-        cfg.blockDim = dim3(PC_THREADS);
-        cfg.dynamicSmemBytes = bytes;
+        cfg.blockDim = dim3(threads);
+        cfg.dynamicSmemBytes = (size_t)optin;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
         at[0].val.clusterDim.x = cs;
@@ -968,17 +1171,16 @@ int choose_dsmem_cluster(int maxRows, size_t* smemBytes) {
         cfg.attrs = at;
         cfg.numAttrs = 1;
         int nc = 0;
-        cudaError_t e = cudaOccupancyMaxActiveClusters(&nc, (const void*)k_precond_dsmem, &cfg);
+        cudaError_t e = cudaOccupancyMaxActiveClusters(&nc, kern, &cfg);
         if (getenv("ASTG_VERBOSE"))
-            fprintf(stderr, "astg: DSMEM preconditioner cluster %d, %zu B smem/CTA: %d clusters (%s)\n", cs, bytes, nc,
-                    cudaGetErrorString(e));
+            fprintf(stderr, "astg: %s preconditioner cluster %d, up to %d B smem/CTA: %d clusters (%s)\n",
+                    async ? "barrier-free" : "level-barrier", cs, optin, nc, cudaGetErrorString(e));
         if (e == cudaSuccess && nc > 0) {
-            *smemBytes = bytes;
+            *smemMax = (size_t)optin;
             return cs;
         }
         cudaGetLastError();
     }
-    *smemBytes = 0;
     return 0;
 }
 static cudaError_t launch_cluster(void (*kern)(Proj, const double*, double*), int csize, cudaStream_t st, Proj P,
@@ -1023,8 +1225,110 @@ int choose_cluster_size(int device) {
     }
     return 0;
 }
+// ---- owner-major schedule of the barrier-free preconditioner.  Rows are dealt to the CTAs in
+// blocks of B = 2^lgB consecutive rows, round robin: row j is computed by, and keeps its value in,
+// CTA (j >> lgB) mod CS at local slot ((j >> (lgB + lgCS)) << lgB) | (j mod B).  Consecutive rows
+// (x neighbours, mostly y neighbours) share a CTA while every dependency level is spread over
+// all CTAs.  Each CTA's rows are sorted by level, so a row's dependencies always come earlier in
+// some CTA's walk.  Keys (owner, level) are counted, scanned and scattered.
+__device__ __forceinline__ int own_of(int j, int lgB, int lgCS) { return (j >> lgB) & ((1 << lgCS) - 1); }
+__device__ __forceinline__ int local_of(int j, int lgB, int lgCS) {
+    return ((j >> (lgB + lgCS)) << lgB) | (j & ((1 << lgB) - 1));
+}
+// column k as (owner CTA << 24 | local slot)
+__device__ __forceinline__ int pack_owner(int k, int lgB, int lgCS) {
+    return (own_of(k, lgB, lgCS) << 24) | local_of(k, lgB, lgCS);
+}
+__global__ void k_own_setup(Proj P, int cs, long long keys) {
+    long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < keys) { P.ownCnt[j] = 0; P.ownFill[j] = 0; }
+    if (j == 0) {
+        int B = 1 << P.pcLgBlock;
+        int blocks = (*P.nDof + B - 1) / B;
+        *P.chunk = ((blocks + cs - 1) / cs) * B;
+    }
+}
+__global__ void k_own_hist(Proj P, int rows1, int lgCS) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *P.nDof) return;
+    atomicAdd(P.ownCnt + (long long)own_of(j, P.pcLgBlock, lgCS) * rows1 + P.level[j], 1);
+}
+__global__ void k_own_scatter(Proj P, int rows1, int lgCS) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *P.nDof) return;
+    long long key = (long long)own_of(j, P.pcLgBlock, lgCS) * rows1 + P.level[j];
+    int p = P.ownPtr[key] + atomicAdd(P.ownFill + key, 1);
+    P.perm[p] = j;
+    P.pos[j] = p;
+}
+__global__ void k_own_bounds(Proj P, int rows1, int cs) {
+    int c = threadIdx.x;
+    if (c < cs) P.ownStart[c] = P.ownPtr[(long long)c * rows1];
+    if (c == cs) P.ownStart[cs] = *P.nDof;
+}
+__global__ void k_own_fill(Proj P, int lgCS) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= *P.nDof) return;
+    int i = P.perm[p];
+    int dg = P.diagPos[i];
+    int lgB = P.pcLgBlock;
+    int cap = P.rowsCap;
+    P.lself[p] = local_of(i, lgB, lgCS);
+    P.linvd[p] = P.invdiag[i];
+    int nf = dg - P.rowPtr[i], nb = P.rowPtr[i + 1] - dg - 1;
+    P.lcntF[p] = nf;
+    P.lcntB[p] = nb;
+    P.cntF[p] = nf;
+    P.cntB[p] = nb;
+    for (int e = 0; e < PC_MAXE; ++e) {
+        int qf = P.rowPtr[i] + e, qb = dg + 1 + e;
+        P.fcolP[(size_t)e * cap + p] = e < nf ? pack_owner(P.col[qf], lgB, lgCS) : 0;
+        P.fvalP[(size_t)e * cap + p] = e < nf ? P.Lv[P.tpos[qf]] : 0.0;
+        P.bcolP[(size_t)e * cap + p] = e < nb ? pack_owner(P.col[qb], lgB, lgCS) : 0;
+        P.bvalP[(size_t)e * cap + p] = e < nb ? P.Lv[qb] : 0.0;
+    }
+}
+// all entries of the row at position p, packed, in the compact arrays (read beyond PC_MAXE)
+__global__ void k_own_overflow(Proj P, int lgCS) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= *P.nDof) return;
+    int i = P.perm[p];
+    int dg = P.diagPos[i];
+    int lgB = P.pcLgBlock;
+    int o = P.fptr[p];
+    for (int q = P.rowPtr[i]; q < dg; ++q, ++o) {
+        P.fcol[o] = pack_owner(P.col[q], lgB, lgCS);
+        P.fval[o] = P.Lv[P.tpos[q]];
+    }
+    o = P.bptr[p];
+    for (int q = dg + 1; q < P.rowPtr[i + 1]; ++q, ++o) {
+        P.bcol[o] = pack_owner(P.col[q], lgB, lgCS);
+        P.bval[o] = P.Lv[q];
+    }
+}
+static void launch_owner_schedule(const Dev& d, Proj& P, cudaStream_t st) {
+    (void)d;
+    int maxRows = P.rowsCap;
+    int cs = P.pcCluster, lgCS = log2_exact(cs);
+    long long keys = (long long)cs * (maxRows + 1);
+    ASTG_LAUNCH(k_own_setup<<<nblk(keys), TB, 0, st>>>(P, cs, keys));
+    ASTG_LAUNCH(k_own_hist<<<nblk(maxRows), TB, 0, st>>>(P, maxRows + 1, lgCS));
+    exclusive_scan(P.ownCnt, P.ownPtr, P.bsum, P.nnz + 1, keys, st);
+    ASTG_LAUNCH(k_own_bounds<<<1, 32, 0, st>>>(P, maxRows + 1, cs));
+    ASTG_LAUNCH(k_own_scatter<<<nblk(maxRows), TB, 0, st>>>(P, maxRows + 1, lgCS));
+    ASTG_LAUNCH(k_own_fill<<<nblk(maxRows), TB, 0, st>>>(P, lgCS));
+    exclusive_scan(P.cntF, P.fptr, P.bsum, P.nnz + 2, maxRows, st);
+    exclusive_scan(P.cntB, P.bptr, P.bsum, P.nnz + 3, maxRows, st);
+    ASTG_LAUNCH(k_level_fptr_last<<<1, 1, 0, st>>>(P));
+    ASTG_LAUNCH(k_own_overflow<<<nblk(maxRows), TB, 0, st>>>(P, lgCS));
+}
+
 void launch_level_schedule(const Dev& d, Proj& P, cudaStream_t st) {
-    int maxRows = d.S + d.H;
+    if (P.pcActive && P.pcAsync) {
+        launch_owner_schedule(d, P, st);
+        return;
+    }
+    int maxRows = P.rowsCap;
     ASTG_LAUNCH(k_level_reset<<<nblk(maxRows + 1), TB, 0, st>>>(P, maxRows));
     ASTG_LAUNCH(k_level_hist<<<nblk(maxRows), TB, 0, st>>>(P));
 
@@ -1163,7 +1467,7 @@ __global__ void k_update_xr(Proj P, double* x, double* r, const double* s, const
         x[i] += alpha * s[i];
         double ri = r[i] + -alpha * z[i];
         r[i] = ri;
-        if (P.pcCluster) P.rl[P.pos[i]] = ri;
+        if (P.pcActive) P.rl[P.pos[i]] = ri;
         v = fabs(ri);
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -1210,10 +1514,24 @@ __global__ void k_update_s(Proj P, double* s, const double* z) {
 __global__ void k_reset_counter(int* c) { *c = 0; }
 
 // one preconditioner application z = (L L^T)^-1 r
+void select_preconditioner(Proj& P, int n) {
+    P.pcActive = 0;
+    P.pcSmem = 0;
+    if (P.pcCluster <= 0 || n <= 0) return;
+    size_t slots = (size_t)((n + P.pcCluster - 1) / P.pcCluster);
+    if (P.pcAsync) {  // whole ownership blocks per CTA
+        size_t B = (size_t)1 << P.pcLgBlock, blocks = (n + B - 1) / B;
+        slots = (blocks + P.pcCluster - 1) / P.pcCluster * B;
+    }
+    size_t bytes = slots * sizeof(double);
+    if (bytes > P.pcSmemMax || n > P.rowsCap) return;
+    P.pcActive = 1;
+    P.pcSmem = bytes;
+}
 static void precond(const Dev& d, Proj& P, const double* r, double* z, int& epoch, cudaStream_t st, KProf* prof) {
-    if (P.pcCluster > 0) {
+    if (P.pcActive) {
         prof_begin(prof, 0, st);
-        cudaError_t e = launch_precond_dsmem(P, r, z, st);
+        cudaError_t e = P.pcAsync ? launch_precond_async(d, P, z, st) : launch_precond_dsmem(P, r, z, st);
         prof_end(prof, st);
         if (e != cudaSuccess) g_cluster_error = e;
         return;
@@ -1241,7 +1559,7 @@ static void precond(const Dev& d, Proj& P, const double* r, double* z, int& epoc
 }
 
 void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st, KProf* prof) {
-    int maxRows = d.S + d.H;
+    int maxRows = P.rowsCap;
     ASTG_LAUNCH(k_mic_init<<<nblk(maxRows), TB, 0, st>>>(P));
     ASTG_LAUNCH(k_reset_counter<<<1, 1, 0, st>>>(P.counter));
     prof_begin(prof, 3, st);
@@ -1253,7 +1571,7 @@ void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epo
 // once when the device "done" flag is set, so a batch that overshoots does no work.
 int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& epoch, int batch, cudaStream_t st,
                     KProf* prof) {
-    int maxRows = d.S + d.H;
+    int maxRows = P.rowsCap;
     int chunks = (maxRows + RED_CHUNK - 1) / RED_CHUNK;
     double* x = P.x;
     double* r = P.r;
@@ -1264,7 +1582,7 @@ int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& e
     cudaMemsetAsync(P.amax, 0, sizeof(unsigned long long), st);
     cudaMemsetAsync(P.done, 0, sizeof(int), st);
     ASTG_LAUNCH(k_absmax<<<nblk(maxRows), TB, 0, st>>>(r, P.nDof, P.amax));
-    if (P.pcCluster) ASTG_LAUNCH(k_to_level_order<<<nblk(maxRows), TB, 0, st>>>(P, r));
+    if (P.pcActive) ASTG_LAUNCH(k_to_level_order<<<nblk(maxRows), TB, 0, st>>>(P, r));
     precond(d, P, r, z, epoch, st, prof);
     ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
     ASTG_LAUNCH(k_pcg_start<<<1, RED_LANES, 0, st>>>(P, P.part, tolFactor));

@@ -126,3 +126,43 @@ def test_standalone_solve_on_reference_systems(name):
             ax[i] = np.dot(val[rp[i]:rp[i + 1]], x[col[rp[i]:rp[i + 1]]])
         assert np.abs(st["b"] - ax).max() <= 1e-6 * np.abs(st["b"]).max() * 1.0000001
     s.close()
+
+
+@pytest.mark.parametrize("mode", ["async", "dsmem", "cluster", "syncfree"])
+def test_every_sweep_form_bit_identical_to_oracle(mode, monkeypatch):
+    """Each form of the MIC(0) triangular sweeps (ASTG_SWEEP) gives the oracle's results bit for
+    bit, and the form asked for is the one that ran (astg_size 7)."""
+    monkeypatch.setenv("ASTG_SWEEP", mode)
+    s = solver(16, 3)
+    o = oracle(16, 3)
+    for k in range(2):
+        s.update(DT)
+        o.step(DT)
+        assert s.last_solve().iterations == int(o.get("pcg_iters")[0])
+        for f in FIELDS + ["tilt_open", "p"]:
+            assert_same(f"{mode}/step{k + 1}/{f}", o.get(f), s.get(f))
+    form = s.size(7)
+    if mode == "async":
+        assert 200 < form < 300
+    elif mode == "dsmem":
+        assert 100 < form < 200
+    elif mode == "cluster":
+        assert 1 < form <= 16
+    else:
+        assert form == 0
+    s.close()
+
+
+def test_full_benchmark_size_step_bit_identical_to_oracle():
+    """256^3-equivalent octree (64^3 coarsest, 3 levels), the size the benchmark runs: one step."""
+    from oracle.oracle import Oracle
+
+    s = solver(64, 3)
+    o = Oracle(64, 3, reduce_mode=1, openmp=True)
+    s.update(DT)
+    o.step(DT)
+    assert s.size(7) > 200  # the barrier-free fused preconditioner ran
+    assert s.last_solve().iterations == int(o.get("pcg_iters")[0])
+    for f in ["density_oct", "heat_oct", "mac", "tilt_vel", "dual_oct", "tilt_open", "p"]:
+        assert_same(f"step1/{f}", o.get(f), s.get(f))
+    s.close()
