@@ -653,6 +653,20 @@ struct astg_handle {
         if (J.pcCluster && J.pcAsync) {
             J.chunk = dalloc<int>(1);
             J.ownStart = dalloc<int>(J.pcCluster + 1);
+            // FP32 copies for the mixed-precision solve
+            J.val32 = dalloc<float>(rows * ROW_W);
+            J.fvalP32 = dalloc<float>(rows * PC_MAXE);
+            J.bvalP32 = dalloc<float>(rows * PC_MAXE);
+            J.linvd32 = dalloc<float>(rows);
+            J.rl32 = dalloc<float>(rows);
+            J.yl32 = dalloc<float>(rows);
+            J.fval32 = dalloc<float>(rows * ROW_W / 2 + 1);
+            J.bval32 = dalloc<float>(rows * ROW_W / 2 + 1);
+            J.e32 = dalloc<float>(rows);
+            J.r32 = dalloc<float>(rows);
+            J.s32 = dalloc<float>(rows);
+            J.z32 = dalloc<float>(rows);
+            J.q32 = dalloc<float>(rows);
             J.lself = dalloc<int>(rows);
             J.yl = dalloc<double>(rows);
             J.ownCnt = dalloc<int>((rows + 1) * J.pcCluster);
@@ -700,13 +714,20 @@ struct astg_handle {
     }
 
     // factorises the system held in the projection workspace and runs the PCG; J.x holds the result
-    void solveCurrent(double tol, int maxIter) {
+    // factorises the system held in the projection workspace and runs the PCG (mixed precision
+    // when asked for and the FP32 preconditioner fits, else FP64); J.x holds the result
+    void solveCurrent(double tol, int maxIter, int precision) {
+        bool mixed = precision == ASTG_MIXED && J.pcActive32;
         launch_factor(d, J, P.omega, P.min_diag, epoch, st, &prof);
-        if (J.clusterSize > 0 || J.pcActive) launch_level_schedule(d, J, st);
+        bool owner = mixed || (J.pcActive && J.pcAsync);
+        if (J.clusterSize > 0 || J.pcActive || mixed) launch_level_schedule(d, J, owner, st);
         ck(cudaEventRecord(evA, st), "event");
-        launch_pcg_fp64(d, J, tol, maxIter, epoch, 8, st, &prof);
+        lastOuter = 0;
+        if (mixed) lastOuter = launch_pcg_mixed(d, J, tol, maxIter, 8, st, &prof);
+        else launch_pcg_fp64(d, J, tol, maxIter, epoch, 8, st, &prof);
         ck(cudaEventRecord(evB, st), "event");
     }
+    int lastOuter = 0;
 
     void project(double dt) {
         Fields& C = F[cur];
@@ -717,7 +738,7 @@ struct astg_handle {
         if (n > J.rowsCap) throw std::runtime_error("projection has more rows than the workspace holds");
         select_preconditioner(J, n);
         launch_assemble(d, C, dOpen, J, dHoPtr, dHoIdx, dt, st);
-        solveCurrent(P.tol, P.max_iter);
+        solveCurrent(P.tol, P.max_iter, P.precision);
         launch_pressure_update(d, C, dOpen, J.pO, J.pT, J.x, dt, st);
         readSolveStats();
     }
@@ -739,7 +760,7 @@ struct astg_handle {
         cudaEventElapsedTime(&ms, evA, evB);
         last.iterations = isc[ISC_ITERS];
         last.converged = isc[ISC_CONVERGED];
-        last.outer = 0;
+        last.outer = lastOuter;
         last.n = n;
         last.nnz = nnz;
         last.residual = sc[SC_RESID];
@@ -750,7 +771,7 @@ struct astg_handle {
     // PCGSolver::solve on a caller-supplied CSR system (uses and overwrites the projection
     // workspace of the handle)
     void solveExternal(int n, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
-                       double* x, double tol, int maxIter, astg_solve_stats* stats) {
+                       double* x, double tol, int maxIter, int precision, astg_solve_stats* stats) {
         long long rows = J.rowsCap;
         if (n <= 0 || n > rows)
             throw std::invalid_argument("astg_solve: n exceeds the handle's capacity (2 x cells + half tilts)");
@@ -769,7 +790,7 @@ struct astg_handle {
         select_preconditioner(J, n);
         launch_external_system(d, J, n, st);
         checkStatus();
-        solveCurrent(tol, maxIter);
+        solveCurrent(tol, maxIter, precision);
         readSolveStats();
         checkStatus();
         ck(cudaMemcpyAsync(x, J.x, sizeof(double) * n, cudaMemcpyDeviceToHost, st), "download");
@@ -1160,7 +1181,7 @@ astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32
                        astg_solve_stats* stats) {
     if (!h || !rowptr || !col || !val || !b || !x || max_iter <= 0) return ASTG_BAD_ARG;
     if (prec != ASTG_FP64 && prec != ASTG_MIXED) return ASTG_BAD_ARG;
-    astg_status s = guard(h, [&] { h->solveExternal(n, rowptr, col, val, b, x, rel_tol, max_iter, stats); });
+    astg_status s = guard(h, [&] { h->solveExternal(n, rowptr, col, val, b, x, rel_tol, max_iter, prec, stats); });
     if (s == ASTG_OK && !h->last.converged) return ASTG_NOT_CONVERGED;
     return s;
 }

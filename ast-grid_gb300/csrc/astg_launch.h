@@ -101,6 +101,22 @@ struct Proj {
     double* fvalP;
     int* bcolP;
     double* bvalP;
+    // mixed precision: FP32 copies of the matrix and of the factor records, FP32 inner vectors
+    int pcActive32;   // the current solve can run the FP32 barrier-free preconditioner
+    size_t pcSmem32;  // its dynamic shared memory per CTA
+    float* val32;     // rowsCap * ROW_W
+    float* fvalP32;   // PC_MAXE * rowsCap
+    float* bvalP32;
+    float* linvd32;
+    float* rl32;
+    float* yl32;
+    float* fval32;    // compact entries
+    float* bval32;
+    float* e32;       // inner correction
+    float* r32;       // inner residual
+    float* s32;
+    float* z32;
+    float* q32;
     size_t pcSmem;   // its dynamic shared memory per CTA in the current solve
     // PCG
     double* x;
@@ -136,7 +152,8 @@ void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWr
 void launch_dof_numbering(const Dev& d, const uint8_t* open, Proj& P, cudaStream_t st);
 void launch_assemble(const Dev& d, const Fields& F, const uint8_t* open, Proj& P, const int* hoPtr, const int* hoIdx,
                      double dt, cudaStream_t st);
-void launch_level_schedule(const Dev& d, Proj& P, cudaStream_t st);
+// owner: the owner-major walk of the barrier-free preconditioner, else the level order
+void launch_level_schedule(const Dev& d, Proj& P, bool owner, cudaStream_t st);
 void launch_external_system(const Dev& d, Proj& P, int rows, cudaStream_t st);
 int choose_cluster_size(int device);
 // cluster size (16 or 8) for the fused preconditioner (barrier-free form when async), or 0
@@ -147,6 +164,9 @@ extern cudaError_t g_cluster_error;  // last failed cluster launch (cudaSuccess 
 void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st, KProf* prof);
 int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& epoch, int batch, cudaStream_t st,
                     KProf* prof);
+// mixed-precision PCG (FP32 inner PCG inside FP64 defect correction); returns the outer cycles, or
+// -1 when the FP32 preconditioner is not available for this solve (nothing was run)
+int launch_pcg_mixed(const Dev& d, Proj& P, double tolFactor, int maxIter, int batch, cudaStream_t st, KProf* prof);
 void launch_pressure_update(const Dev& d, const Fields& F, const uint8_t* open, const int* pO, const int* pT,
                             const double* p, double dt, cudaStream_t st);
 void launch_dual(const Dev& d, const Fields& F, cudaStream_t st);

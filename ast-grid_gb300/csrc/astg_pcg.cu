@@ -14,7 +14,9 @@
 // DS_WAIT_TIMEOUT in the device status word and carries on, so a wait can never hang the GPU.
 #include <cooperative_groups.h>
 #include <cstdio>
+#include <algorithm>
 #include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 #include "astg_launch.h"
@@ -931,118 +933,156 @@ __global__ void __launch_bounds__(256, 1) k_precond_dsmem(Proj P, double* z, int
 // waiting everywhere and finishes with invalid values.  Per row the operations are the
 // reference's, in the reference's order.
 constexpr int PCA_THREADS = 256;
-constexpr unsigned long long PCA_EMPTY = 0x7FF4DEADBEEF0001ull;
 constexpr long long PCA_SPIN_LIMIT = 1LL << 22;
-// Polls are plain (weak) shared-memory loads kept in place by asm volatile: shared memory is not
-// cached, so each one reads the slot's current contents, and an aligned 8-byte store is seen
-// whole or not at all.  The value itself is the signal, so nothing else needs ordering; the cluster
-// barrier at the end of each sweep orders everything for what follows.  (Loads with .relaxed.cluster
-// semantics measured about 20x slower per polling pass with every warp of the cluster polling.)
-__device__ __forceinline__ unsigned long long pca_ld_remote(uint32_t a) {
-    unsigned long long v;
-    asm volatile("ld.shared::cluster.b64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
-    return v;
-}
-__device__ __forceinline__ void pca_st_local(uint32_t a, double v) {
-    asm volatile("st.shared.b64 [%0], %1;" ::"r"(a), "l"((unsigned long long)__double_as_longlong(v)) : "memory");
-}
-struct PcaRow {
+// Value-type traits of the barrier-free preconditioner (FP64 drop-in form, FP32 inner solve of the
+// mixed-precision form).  EMPTY is a signalling-NaN bit pattern: no floating-point operation
+// produces it (arithmetic on a NaN returns a quiet NaN).
+template <typename T> struct Pca;
+template <> struct Pca<double> {
+    typedef unsigned long long Bits;
+    static constexpr Bits EMPTY = 0x7FF4DEADBEEF0001ull;
+    // Polls are plain (weak) shared-memory loads kept in place by asm volatile: shared memory is
+    // not cached, so each one reads the slot's current contents, and an aligned store is seen
+    // whole or not at all.  The value itself is the signal, so nothing else needs ordering; the
+    // cluster barrier at the end of each sweep orders everything for what follows.  (Loads with
+    // .relaxed.cluster semantics measured about 20x slower per polling pass with every warp of
+    // the cluster polling.)
+    static __device__ __forceinline__ Bits ld(uint32_t a) {
+        Bits v;
+        asm volatile("ld.shared::cluster.b64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
+        return v;
+    }
+    static __device__ __forceinline__ void st(uint32_t a, double v) {
+        asm volatile("st.shared.b64 [%0], %1;" ::"r"(a), "l"((Bits)__double_as_longlong(v)) : "memory");
+    }
+    static __device__ __forceinline__ double val(Bits b) { return __longlong_as_double((long long)b); }
+};
+template <> struct Pca<float> {
+    typedef unsigned int Bits;
+    static constexpr Bits EMPTY = 0x7FA5DEADu;
+    static __device__ __forceinline__ Bits ld(uint32_t a) {
+        Bits v;
+        asm volatile("ld.shared::cluster.b32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+        return v;
+    }
+    static __device__ __forceinline__ void st(uint32_t a, float v) {
+        asm volatile("st.shared.b32 [%0], %1;" ::"r"(a), "r"(__float_as_uint(v)) : "memory");
+    }
+    static __device__ __forceinline__ float val(Bits b) { return __uint_as_float(b); }
+};
+// per-precision arrays of the preconditioner (the schedule and columns are shared)
+template <typename T> struct PcaData {
+    const T* fvalP;  // PC_MAXE x rowsCap, level-ordered factor values (forward / backward)
+    const T* bvalP;
+    const T* linvd;  // pivot reciprocals at each position
+    const T* rl;     // right-hand side at each position
+    T* yl;           // forward result at each position
+    const T* fval;   // compact entries (read beyond PC_MAXE)
+    const T* bval;
+};
+template <typename T> struct PcaRow {
     int p, self, cnt;
-    double rhs, invd;
+    T rhs, invd;
     int col[PC_MAXE];
-    double val[PC_MAXE];
+    T val[PC_MAXE];
 };
 // record of position p (valid when q < cnt): independent loads only
-__device__ __forceinline__ void pca_load(const Proj& P, int base, int q, int rows, bool fwd, PcaRow& w) {
+template <typename T>
+__device__ __forceinline__ void pca_load(const Proj& P, const PcaData<T>& D, int base, int q, int rows, bool fwd,
+                                         PcaRow<T>& w) {
     w.cnt = -1;
     if (q < 0 || q >= rows) return;
     const int p = base + q;
     const int cap = P.rowsCap;
     const int* cc = fwd ? P.fcolP : P.bcolP;
-    const double* vv = fwd ? P.fvalP : P.bvalP;
+    const T* vv = fwd ? D.fvalP : D.bvalP;
     w.p = p;
     w.self = P.lself[p];
     w.cnt = fwd ? P.lcntF[p] : P.lcntB[p];
-    w.invd = P.linvd[p];
-    w.rhs = fwd ? P.rl[p] : P.yl[p];
+    w.invd = D.linvd[p];
+    w.rhs = fwd ? D.rl[p] : D.yl[p];
 #pragma unroll
     for (int e = 0; e < PC_MAXE; ++e) {
         w.col[e] = cc[(size_t)e * cap + p];
         w.val[e] = vv[(size_t)e * cap + p];
     }
 }
-// One row per lane; the warp polls until every lane's row is done.  A lane consumes its entries
-// strictly in order (the reference's order) as far as they hold values, and stores its row the
-// moment the last one arrives, so no lane ever waits for a lane of its own warp while holding its
+// One row per lane; the warp polls until every lane's row is done.  A lane stores its row the
+// moment its last entry arrives, so no lane ever waits for a lane of its own warp while holding its
 // own result back.  The loop and its exit are warp-uniform.  Entry addresses are resolved once per
 // row into the cluster's shared-memory window (mapa), so every poll is one load form for local
 // and remote entries alike; every pass re-loads all entries still missing, so they resolve in
 // parallel.  Bounded: after PCA_SPIN_LIMIT polls (or once any wait of the launch has given up) the
 // warp stops waiting and reports.
-__device__ __forceinline__ uint32_t pca_window(uint32_t own, int packed) {
-    uint32_t a = own + (uint32_t)(packed & 0xffffff) * 8u, m;
+__device__ __forceinline__ uint32_t pca_window(uint32_t own, int packed, uint32_t esize) {
+    uint32_t a = own + (uint32_t)(packed & 0xffffff) * esize, m;
     asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(m) : "r"(a), "r"((uint32_t)(packed >> 24)));
     return m;
 }
 constexpr int PCA_MAXE = 2 * PC_MAXE;  // entries a row resolves in registers (8 from the record)
 // The polling pass is integer-only: it re-loads the entries not yet known to hold values and
-// extends the prefix of present ones.  The FP64 arithmetic runs once per row, after every entry is
+// extends the prefix of present ones.  The arithmetic runs once per row, after every entry is
 // present, in the reference's order (FP64 issue is scarce on this part, and predicated-off FP64
 // instructions in a polling pass would still occupy the FP64 pipe on every pass).
-__device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaRow& w, bool fwd, uint32_t own, int* status) {
+template <typename T>
+__device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaData<T>& D, const PcaRow<T>& w, bool fwd,
+                                              uint32_t own, int* status) {
+    typedef Pca<T> K;
+    typedef typename K::Bits Bits;
+    const uint32_t es = sizeof(T);
     bool done = w.cnt < 0;
     uint32_t a[PCA_MAXE];
-    double val[PCA_MAXE];
+    T val[PCA_MAXE];
 #pragma unroll
     for (int e = 0; e < PC_MAXE; ++e) {
-        a[e] = pca_window(own, w.col[e]);
+        a[e] = pca_window(own, w.col[e], es);
         val[e] = w.val[e];
     }
     // entries 8..15 of a longer row: loaded once, together, before any polling
     const int* oc = fwd ? P.fcol : P.bcol;
-    const double* ov = fwd ? P.fval : P.bval;
+    const T* ov = fwd ? D.fval : D.bval;
     const int q0 = (!done && w.cnt > PC_MAXE) ? (fwd ? P.fptr : P.bptr)[w.p] : 0;
 #pragma unroll
     for (int e = PC_MAXE; e < PCA_MAXE; ++e) {
         bool has = e < w.cnt;
-        a[e] = pca_window(own, has ? oc[q0 + e] : 0);
-        val[e] = has ? ov[q0 + e] : 0.0;
+        a[e] = pca_window(own, has ? oc[q0 + e] : 0, es);
+        val[e] = has ? ov[q0 + e] : T(0);
     }
     const int lim = min(w.cnt, PCA_MAXE);
-    unsigned long long v[PCA_MAXE];
+    Bits v[PCA_MAXE];
     int got = 0;        // leading entries known to hold values
     bool part = false;  // the first lim entries are accumulated (rows longer than PCA_MAXE)
-    double acc = w.rhs;
+    T acc = w.rhs;
     for (long long it = 0;; ++it) {
         if (!done) {
             if (!part) {
                 const int g0 = got;
 #pragma unroll
                 for (int e = 0; e < PCA_MAXE; ++e)
-                    if (e >= g0 && e < lim) v[e] = pca_ld_remote(a[e]);
+                    if (e >= g0 && e < lim) v[e] = K::ld(a[e]);
 #pragma unroll
                 for (int e = 0; e < PCA_MAXE; ++e)
-                    if (e == got && e < lim && v[e] != PCA_EMPTY) got = e + 1;
+                    if (e == got && e < lim && v[e] != K::EMPTY) got = e + 1;
                 if (got == lim) {
 #pragma unroll
                     for (int e = 0; e < PCA_MAXE; ++e) {
                         if (e >= lim) break;
-                        acc = acc - val[e] * __longlong_as_double((long long)v[e]);
+                        acc = acc - val[e] * K::val(v[e]);
                     }
                     part = true;
                 }
             }
             // rows longer than PCA_MAXE entries: the rest one at a time from the compact arrays
             while (part && got < w.cnt) {
-                unsigned long long x = pca_ld_remote(pca_window(own, oc[q0 + got]));
-                if (x == PCA_EMPTY) break;
-                acc = acc - ov[q0 + got] * __longlong_as_double((long long)x);
+                Bits x = K::ld(pca_window(own, oc[q0 + got], es));
+                if (x == K::EMPTY) break;
+                acc = acc - ov[q0 + got] * K::val(x);
                 ++got;
             }
             if (part && got >= w.cnt) {
-                double y = acc * w.invd;
-                if (fwd) P.yl[w.p] = y;
-                pca_st_local(own + (uint32_t)w.self * 8u, y);
+                T y = acc * w.invd;
+                if (fwd) D.yl[w.p] = y;
+                K::st(own + (uint32_t)w.self * es, y);
                 done = true;
             }
         }
@@ -1054,18 +1094,21 @@ __device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaRow& w, bo
         }
     }
 }
-__global__ void __launch_bounds__(PCA_THREADS, 1) k_precond_async(Proj P, double* z, int* status, int lgCS) {
+template <typename T>
+__global__ void __launch_bounds__(PCA_THREADS, 1) k_precond_async(Proj P, PcaData<T> D, T* z, int* status, int lgCS) {
+    typedef Pca<T> K;
     if (*P.done) return;
-    extern __shared__ double zsh[];
+    extern __shared__ __align__(16) unsigned char pca_smem[];
+    typename K::Bits* zraw = reinterpret_cast<typename K::Bits*>(pca_smem);
+    T* zsh = reinterpret_cast<T*>(pca_smem);
     cg::cluster_group cl = cg::this_cluster();
     const int rank = cl.block_rank();
     const int n = *P.nDof, chunk = *P.chunk;
     const int base = P.ownStart[rank];
     const int rows = P.ownStart[rank + 1] - base;
     const int lgB = P.pcLgBlock;
-    const uint32_t own = (uint32_t)__cvta_generic_to_shared(zsh);
-    unsigned long long* zraw = reinterpret_cast<unsigned long long*>(zsh);
-    for (int l = threadIdx.x; l < chunk; l += blockDim.x) zraw[l] = PCA_EMPTY;
+    const uint32_t own = (uint32_t)__cvta_generic_to_shared(pca_smem);
+    for (int l = threadIdx.x; l < chunk; l += blockDim.x) zraw[l] = K::EMPTY;
     cl.sync();  // every CTA is running and every slot of the cluster is empty
     for (int dir = 0; dir < 2; ++dir) {
         const bool fwd = dir == 0;
@@ -1074,22 +1117,22 @@ __global__ void __launch_bounds__(PCA_THREADS, 1) k_precond_async(Proj P, double
         auto qof = [&](int k) { return fwd ? k : rows - 1 - k; };
         // thread t takes entries t, t + blockDim, ...: the same number of rounds for every thread,
         // so warps stay whole; the next record is loaded while the current row waits
-        const int T = (int)blockDim.x;
-        const int rounds = (rows + T - 1) / T;
+        const int T_ = (int)blockDim.x;
+        const int rounds = (rows + T_ - 1) / T_;
         auto pick = [&](int k) {
-            int q = threadIdx.x + k * T;
+            int q = threadIdx.x + k * T_;
             return q < rows ? qof(q) : -1;
         };
-        PcaRow W, X;
-        pca_load(P, base, pick(0), rows, fwd, W);
+        PcaRow<T> W, X;
+        pca_load(P, D, base, pick(0), rows, fwd, W);
         for (int k = 0; k < rounds; ++k) {
-            pca_load(P, base, pick(k + 1), rows, fwd, X);
-            pca_solve_row(P, W, fwd, own, status);
+            pca_load(P, D, base, pick(k + 1), rows, fwd, X);
+            pca_solve_row(P, D, W, fwd, own, status);
             W = X;
         }
         cl.sync();  // sweep finished everywhere (global and shared writes ordered at cluster scope)
         if (fwd) {
-            for (int l = threadIdx.x; l < chunk; l += blockDim.x) zraw[l] = PCA_EMPTY;
+            for (int l = threadIdx.x; l < chunk; l += blockDim.x) zraw[l] = K::EMPTY;
             cl.sync();
         }
     }
@@ -1112,17 +1155,17 @@ static cudaError_t launch_precond_dsmem(const Proj& P, const double* r, double* 
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    int lg = 0;
-    while ((1 << lg) < P.pcCluster) ++lg;
     ++g_launches;
     (void)r;
-    return cudaLaunchKernelEx(&cfg, k_precond_dsmem, P, z, lg);
+    return cudaLaunchKernelEx(&cfg, k_precond_dsmem, P, z, log2_exact(P.pcCluster));
 }
-static cudaError_t launch_precond_async(const Dev& d, const Proj& P, double* z, cudaStream_t st) {
+template <typename T>
+static cudaError_t launch_precond_async(const Dev& d, const Proj& P, const PcaData<T>& D, T* z, size_t smem,
+                                       cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(P.pcCluster);
     cfg.blockDim = dim3(PCA_THREADS);
-    cfg.dynamicSmemBytes = P.pcSmem;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1132,14 +1175,17 @@ static cudaError_t launch_precond_async(const Dev& d, const Proj& P, double* z, 
     cfg.attrs = at;
     cfg.numAttrs = 1;
     ++g_launches;
-    return cudaLaunchKernelEx(&cfg, k_precond_async, P, z, d.status, log2_exact(P.pcCluster));
+    return cudaLaunchKernelEx(&cfg, k_precond_async<T>, P, D, z, d.status, log2_exact(P.pcCluster));
+}
+static PcaData<double> pca_data64(const Proj& P) {
+    return PcaData<double>{P.fvalP, P.bvalP, P.linvd, P.rl, P.yl, P.fval, P.bval};
 }
 // Cluster size (16, else 8) at which the fused preconditioner (barrier-free form when async) can
 // run with the largest dynamic shared memory a CTA may have, or 0; *smemMax = that largest size.
 // Each solve then uses ceil(n / CS) doubles per CTA and falls back to the global-memory sweeps
 // when they do not fit.
 int choose_dsmem_cluster(bool async, size_t* smemMax) {
-    const void* kern = async ? (const void*)k_precond_async : (const void*)k_precond_dsmem;
+    const void* kern = async ? (const void*)k_precond_async<double> : (const void*)k_precond_dsmem;
     const int threads = async ? PCA_THREADS : PC_THREADS;
     *smemMax = 0;
     cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -1157,6 +1203,14 @@ int choose_dsmem_cluster(bool async, size_t* smemMax) {
     if (optin <= 0 || cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
         cudaGetLastError();
         return 0;
+    }
+    if (async) {  // the FP32 instance of the mixed-precision solve: same launch shape
+        const void* k32 = (const void*)k_precond_async<float>;
+        cudaFuncSetAttribute(k32, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (cudaFuncSetAttribute(k32, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
     }
     for (int cs : {16, 8}) {
         cudaLaunchConfig_t cfg = {};
@@ -1286,7 +1340,12 @@ __global__ void k_own_fill(Proj P, int lgCS) {
         P.fvalP[(size_t)e * cap + p] = e < nf ? P.Lv[P.tpos[qf]] : 0.0;
         P.bcolP[(size_t)e * cap + p] = e < nb ? pack_owner(P.col[qb], lgB, lgCS) : 0;
         P.bvalP[(size_t)e * cap + p] = e < nb ? P.Lv[qb] : 0.0;
+        if (P.fvalP32) {  // the factor is computed in FP64 and rounded once
+            P.fvalP32[(size_t)e * cap + p] = (float)P.fvalP[(size_t)e * cap + p];
+            P.bvalP32[(size_t)e * cap + p] = (float)P.bvalP[(size_t)e * cap + p];
+        }
     }
+    if (P.linvd32) P.linvd32[p] = (float)P.invdiag[i];
 }
 // all entries of the row at position p, packed, in the compact arrays (read beyond PC_MAXE)
 __global__ void k_own_overflow(Proj P, int lgCS) {
@@ -1299,11 +1358,13 @@ __global__ void k_own_overflow(Proj P, int lgCS) {
     for (int q = P.rowPtr[i]; q < dg; ++q, ++o) {
         P.fcol[o] = pack_owner(P.col[q], lgB, lgCS);
         P.fval[o] = P.Lv[P.tpos[q]];
+        if (P.fval32) P.fval32[o] = (float)P.fval[o];
     }
     o = P.bptr[p];
     for (int q = dg + 1; q < P.rowPtr[i + 1]; ++q, ++o) {
         P.bcol[o] = pack_owner(P.col[q], lgB, lgCS);
         P.bval[o] = P.Lv[q];
+        if (P.bval32) P.bval32[o] = (float)P.bval[o];
     }
 }
 static void launch_owner_schedule(const Dev& d, Proj& P, cudaStream_t st) {
@@ -1323,8 +1384,8 @@ static void launch_owner_schedule(const Dev& d, Proj& P, cudaStream_t st) {
     ASTG_LAUNCH(k_own_overflow<<<nblk(maxRows), TB, 0, st>>>(P, lgCS));
 }
 
-void launch_level_schedule(const Dev& d, Proj& P, cudaStream_t st) {
-    if (P.pcActive && P.pcAsync) {
+void launch_level_schedule(const Dev& d, Proj& P, bool owner, cudaStream_t st) {
+    if (owner) {
         launch_owner_schedule(d, P, st);
         return;
     }
@@ -1517,6 +1578,8 @@ __global__ void k_reset_counter(int* c) { *c = 0; }
 void select_preconditioner(Proj& P, int n) {
     P.pcActive = 0;
     P.pcSmem = 0;
+    P.pcActive32 = 0;
+    P.pcSmem32 = 0;
     if (P.pcCluster <= 0 || n <= 0) return;
     size_t slots = (size_t)((n + P.pcCluster - 1) / P.pcCluster);
     if (P.pcAsync) {  // whole ownership blocks per CTA
@@ -1524,14 +1587,20 @@ void select_preconditioner(Proj& P, int n) {
         slots = (blocks + P.pcCluster - 1) / P.pcCluster * B;
     }
     size_t bytes = slots * sizeof(double);
-    if (bytes > P.pcSmemMax || n > P.rowsCap) return;
+    if (n > P.rowsCap) return;
+    if (P.pcAsync && P.val32 && slots * sizeof(float) <= P.pcSmemMax) {
+        P.pcActive32 = 1;
+        P.pcSmem32 = slots * sizeof(float);
+    }
+    if (bytes > P.pcSmemMax) return;
     P.pcActive = 1;
     P.pcSmem = bytes;
 }
 static void precond(const Dev& d, Proj& P, const double* r, double* z, int& epoch, cudaStream_t st, KProf* prof) {
     if (P.pcActive) {
         prof_begin(prof, 0, st);
-        cudaError_t e = P.pcAsync ? launch_precond_async(d, P, z, st) : launch_precond_dsmem(P, r, z, st);
+        cudaError_t e = P.pcAsync ? launch_precond_async(d, P, pca_data64(P), z, P.pcSmem, st)
+                                  : launch_precond_dsmem(P, r, z, st);
         prof_end(prof, st);
         if (e != cudaSuccess) g_cluster_error = e;
         return;
@@ -1614,4 +1683,209 @@ int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& e
     return launched;
 }
 
+}  // namespace astg
+
+namespace astg {
+// ------------------------------------------------------------------ mixed-precision PCG
+// Defect correction: x = 0, r = b; while |r|_inf > tol |b|_inf: solve A e = r with an FP32 PCG
+// (FP32 matrix, FP32 MIC(0) factor rounded from the FP64 one, FP32 vectors; dot products reduced
+// in FP64 by the fixed tree; alpha and beta in FP64) until its residual drops below
+// max(1e-5 |r|_inf, 0.5 tol |b|_inf), then x += e and r = b - A x in FP64.  The stopping test is
+// the reference's, on the FP64 residual.
+constexpr double MIXED_INNER_REDUCTION = 1e-5;
+constexpr int MIXED_MAX_OUTER = 20;
+__global__ void k_to_f32(const double* a, float* b, const int* nptr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *nptr) b[i] = (float)a[i];
+}
+// r = b - A x (FP64, row sums in column order), |r|_inf into amax
+__global__ void k_resid64(Proj P, const double* x, double* r) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0;
+    if (i < *P.nDof) {
+        double t = 0;
+        for (int q = P.rowPtr[i]; q < P.rowPtr[i + 1]; ++q) t += P.val[q] * x[P.col[q]];
+        double ri = P.b[i] - t;
+        r[i] = ri;
+        v = fabs(ri);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        double w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(P.amax, (unsigned long long)__double_as_longlong(v));
+}
+// start of an inner solve: r32 = r (also in walk order), e32 = 0
+__global__ void k_inner_init(Proj P, const double* r) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *P.nDof) return;
+    float ri = (float)r[i];
+    P.r32[i] = ri;
+    P.rl32[P.pos[i]] = ri;
+    P.e32[i] = 0.0f;
+}
+// partial dots of FP32 vectors, products and sums in FP64 (fixed tree)
+__global__ void k_tree_dot32(const float* a, const float* b, const int* nptr, double* part) {
+    __shared__ double sh[RED_LANES];
+    long long n = *nptr;
+    long long base = (long long)blockIdx.x * RED_CHUNK;
+    if (base >= n && blockIdx.x > 0) return;
+    double acc = 0.0;
+    for (int k = 0; k < RED_PER_LANE; ++k) {
+        long long i = base + threadIdx.x + (long long)RED_LANES * k;
+        if (i < n) acc = acc + (double)a[i] * (double)b[i];
+    }
+    double r = block_tree(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+// inner start: rho = z.r, tolerance of this inner solve; the iteration count carries on
+__global__ void k_inner_start(Proj P, const double* partRho, double innerTol) {
+    __shared__ double sh[RED_LANES];
+    int n = *P.nDof;
+    long long m = (n + RED_CHUNK - 1) / RED_CHUNK;
+    double rho = fold_partials(partRho, m, sh);
+    if (threadIdx.x == 0) {
+        P.sc[SC_TOL] = innerTol;
+        P.sc[SC_RHO] = rho;
+        *P.done = (rho == 0 || rho != rho) ? 1 : 0;
+        *P.amax = 0;
+    }
+}
+__global__ void k_copy32(const float* a, float* b, const int* nptr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *nptr) b[i] = a[i];
+}
+// q = A32 s (FP32 row sums), partial dots s.q in FP64
+__global__ void k_spmv32_dot(Proj P, const float* s, float* q, double* part) {
+    __shared__ double sh[RED_LANES];
+    if (*P.done) return;
+    int n = *P.nDof;
+    long long base = (long long)blockIdx.x * RED_CHUNK;
+    if (base >= n) return;
+    double acc = 0.0;
+    for (int k = 0; k < RED_PER_LANE; ++k) {
+        long long i = base + threadIdx.x + (long long)RED_LANES * k;
+        if (i < n) {
+            float t = 0;
+            for (int c = P.rowPtr[i]; c < P.rowPtr[i + 1]; ++c) t += P.val32[c] * s[P.col[c]];
+            q[i] = t;
+            acc = acc + (double)s[i] * (double)t;
+        }
+    }
+    double r = block_tree(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+__global__ void k_update_er32(Proj P) {
+    if (*P.done) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float alpha = (float)P.sc[SC_ALPHA];
+    double v = 0;
+    if (i < *P.nDof) {
+        P.e32[i] += alpha * P.s32[i];
+        float ri = P.r32[i] - alpha * P.q32[i];
+        P.r32[i] = ri;
+        P.rl32[P.pos[i]] = ri;
+        v = fabs((double)ri);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        double w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(P.amax, (unsigned long long)__double_as_longlong(v));
+}
+__global__ void k_update_s32(Proj P) {
+    if (*P.done) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *P.nDof) P.s32[i] = P.z32[i] + (float)P.sc[SC_BETA] * P.s32[i];
+}
+__global__ void k_add_correction(Proj P, double* x) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *P.nDof) x[i] += (double)P.e32[i];
+}
+__global__ void k_mixed_finish(Proj P, double res, double tolAbs, double res0, int converged) {
+    P.sc[SC_RESID0] = res0;
+    P.sc[SC_RESID] = res;
+    P.sc[SC_TOL] = tolAbs;
+    P.isc[ISC_CONVERGED] = converged;
+}
+static PcaData<float> pca_data32(const Proj& P) {
+    return PcaData<float>{P.fvalP32, P.bvalP32, P.linvd32, P.rl32, P.yl32, P.fval32, P.bval32};
+}
+static double read_amax(Proj& P, cudaStream_t st) {
+    unsigned long long bits = 0;
+    cudaMemcpyAsync(&bits, P.amax, sizeof bits, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    double v;
+    memcpy(&v, &bits, sizeof v);
+    return v;
+}
+int launch_pcg_mixed(const Dev& d, Proj& P, double tolFactor, int maxIter, int batch, cudaStream_t st, KProf* prof) {
+    if (!P.pcActive32) return -1;
+    int maxRows = P.rowsCap;
+    int chunks = (maxRows + RED_CHUNK - 1) / RED_CHUNK;
+    double* x = P.x;
+    double* r = P.r;
+    ASTG_LAUNCH(k_to_f32<<<nblk((long long)maxRows * ROW_W), TB, 0, st>>>(P.val, P.val32, P.nnz));
+    ASTG_LAUNCH(k_zero_vec<<<nblk(maxRows), TB, 0, st>>>(x, P.nDof));
+    ASTG_LAUNCH(k_copy<<<nblk(maxRows), TB, 0, st>>>(P.b, r, P.nDof));
+    cudaMemsetAsync(P.amax, 0, sizeof(unsigned long long), st);
+    cudaMemsetAsync(P.isc, 0, sizeof(int) * ISC_COUNT, st);
+    ASTG_LAUNCH(k_absmax<<<nblk(maxRows), TB, 0, st>>>(r, P.nDof, P.amax));
+    const double res0 = read_amax(P, st);
+    const double tolAbs = tolFactor * res0;
+    double res = res0;
+    int outer = 0, converged = 0;
+    PcaData<float> D = pca_data32(P);
+    for (;;) {
+        if (res <= tolAbs) {
+            converged = 1;
+            break;
+        }
+        int iters = 0;
+        cudaMemcpyAsync(&iters, P.isc + ISC_ITERS, sizeof iters, cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        if (outer >= MIXED_MAX_OUTER || iters >= maxIter || res != res) break;
+        double innerTol = std::max(MIXED_INNER_REDUCTION * res, 0.5 * tolAbs);
+        ASTG_LAUNCH(k_inner_init<<<nblk(maxRows), TB, 0, st>>>(P, r));
+        cudaMemsetAsync(P.done, 0, sizeof(int), st);
+        prof_begin(prof, 0, st);
+        cudaError_t e = launch_precond_async(d, P, D, P.z32, P.pcSmem32, st);
+        prof_end(prof, st);
+        if (e != cudaSuccess) g_cluster_error = e;
+        ASTG_LAUNCH(k_tree_dot32<<<chunks, RED_LANES, 0, st>>>(P.z32, P.r32, P.nDof, P.part));
+        ASTG_LAUNCH(k_inner_start<<<1, RED_LANES, 0, st>>>(P, P.part, innerTol));
+        ASTG_LAUNCH(k_copy32<<<nblk(maxRows), TB, 0, st>>>(P.z32, P.s32, P.nDof));
+        for (int launched = 0; launched < maxIter;) {
+            for (int it = 0; it < batch; ++it) {
+                prof_begin(prof, 2, st);
+                ASTG_LAUNCH(k_spmv32_dot<<<chunks, RED_LANES, 0, st>>>(P, P.s32, P.q32, P.part));
+                prof_end(prof, st);
+                ASTG_LAUNCH(k_alpha<<<1, RED_LANES, 0, st>>>(P, P.part));
+                ASTG_LAUNCH(k_update_er32<<<nblk(maxRows), TB, 0, st>>>(P));
+                ASTG_LAUNCH(k_check<<<1, 1, 0, st>>>(P, maxIter));
+                prof_begin(prof, 0, st);
+                e = launch_precond_async(d, P, D, P.z32, P.pcSmem32, st);
+                prof_end(prof, st);
+                if (e != cudaSuccess) g_cluster_error = e;
+                ASTG_LAUNCH(k_tree_dot32<<<chunks, RED_LANES, 0, st>>>(P.z32, P.r32, P.nDof, P.part));
+                ASTG_LAUNCH(k_beta<<<1, RED_LANES, 0, st>>>(P, P.part));
+                ASTG_LAUNCH(k_update_s32<<<nblk(maxRows), TB, 0, st>>>(P));
+            }
+            launched += batch;
+            cudaMemcpyAsync(P.hostDone, P.done, sizeof(int), cudaMemcpyDeviceToHost, st);
+            cudaStreamSynchronize(st);
+            prof_drain(prof);
+            if (*P.hostDone) break;
+        }
+        ASTG_LAUNCH(k_add_correction<<<nblk(maxRows), TB, 0, st>>>(P, x));
+        cudaMemsetAsync(P.amax, 0, sizeof(unsigned long long), st);
+        prof_begin(prof, 2, st);
+        ASTG_LAUNCH(k_resid64<<<nblk(maxRows), TB, 0, st>>>(P, x, r));
+        prof_end(prof, st);
+        res = read_amax(P, st);
+        ++outer;
+    }
+    ASTG_LAUNCH(k_mixed_finish<<<1, 1, 0, st>>>(P, res, tolAbs, res0, converged));
+    return outer;
+}
 }  // namespace astg
