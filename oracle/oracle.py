@@ -70,6 +70,9 @@ def lib(openmp=False):
         _lib.orc_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_longlong]
         _lib.orc_set.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_longlong]
         _lib.orc_size.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        _lib.orc_extrapolate.restype = ctypes.c_longlong
+        _lib.orc_extrapolate.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_double]
         _lib.orc_solve.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 5 + [ctypes.c_double,
                                                                                                ctypes.c_int]
         _libs[openmp] = _lib
@@ -143,6 +146,18 @@ class Oracle:
         it = self._lib.orc_solve(self._h, len(bb), rp.ctypes.data, c.ctypes.data, v.ctypes.data, bb.ctypes.data,
                                  x.ctypes.data, tol, max_iter)
         return x, it
+
+    def extrapolate(self, field, sdf, offset=0.0, max_distance_factor=4.0):
+        """FmmLevelSetSolver3::extrapolate of "density" or "heat" in place from the nodes where
+        sdf < -offset * d; sdf is res^3 (index (z*res + y)*res + x).  Returns the nodes assigned."""
+        g = np.ascontiguousarray(sdf, dtype=np.float64).ravel()
+        res = round(len(g) ** (1.0 / 3.0))
+        if res ** 3 != len(g):
+            raise ValueError("sdf must hold res^3 values")
+        n = self._lib.orc_extrapolate(self._h, field.encode(), g.ctypes.data, res, offset, max_distance_factor)
+        if n < 0:
+            raise ValueError("oracle: bad extrapolation argument")
+        return n
 
     @property
     def slots(self):

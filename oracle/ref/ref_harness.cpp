@@ -21,6 +21,7 @@
 #include "octree_omnigrid_solver3.h"
 #include "octree_util.h"
 #include "advection.h"
+#include "jet/fmm_levelset_solver3.h"
 #include "scene.h"
 
 #include <cstdio>
@@ -86,6 +87,10 @@ struct Options {
     double dt = 0.01, tol = 1e-6, noise = 1e-3, buoyD = -0.1, buoyT = 1.0, decay = 1.0;
     uint64_t seed = 0;
     bool stages = false;
+    // FmmLevelSetSolver3::extrapolate of the density after the steps: sphere SDF (centre, radius),
+    // maximum distance factor, validity offset (known where sdf < -offset * d)
+    bool extrap = false;
+    double exC[3] = {0, 0, 0}, exR = 0, exMax = 0, exOff = 0;
     std::string out = "ref_out";
     astg_scene::Sphere src = astg_scene::default_source();
 };
@@ -455,6 +460,11 @@ int main(int argc, char** argv) {
         else if (a == "--stages") o.stages = true;
         else if (a == "--out") o.out = next();
         else if (a == "--source") parseSource(next(), o.src);
+        else if (a == "--extrapolate") {
+            o.extrap = true;
+            if (sscanf(next(), "%lf,%lf,%lf,%lf,%lf,%lf", &o.exC[0], &o.exC[1], &o.exC[2], &o.exR, &o.exMax, &o.exOff) != 6)
+                throw std::runtime_error("--extrapolate cx,cy,cz,r,max_distance_factor,offset");
+        }
         else throw std::runtime_error("unknown option " + a);
     }
     spdlog::set_level(spdlog::level::err);
@@ -493,5 +503,35 @@ int main(int argc, char** argv) {
     }
     for (int l = 0; l < h.levels(); ++l)
         if (h.getLayout()->levelSize(l) != sizes0[l]) fprintf(stderr, "warning: level %d grew during the run\n", l);
+    if (o.extrap) {
+        // sphere signed distance at the finest cell centres, sampled by the reference's trilinear
+        // CellCenteredGrid::sample; the density is extrapolated in place (input and output are one grid)
+        auto sdf = std::make_shared<CellCenteredScalarGrid3>(Size3(res, res, res), 1.0 / res, 0.0);
+        std::vector<double> sv((size_t)res * res * res);
+        for (int z = 0; z < res; ++z)
+            for (int y = 0; y < res; ++y)
+                for (int x = 0; x < res; ++x) {
+                    double p[3] = {(x + 0.5) / res, (y + 0.5) / res, (z + 0.5) / res};
+                    double dx = p[0] - o.exC[0], dy = p[1] - o.exC[1], dz = p[2] - o.exC[2];
+                    double v = std::sqrt(dx * dx + dy * dy + dz * dz) - o.exR;
+                    sdf->set(x, y, z, v);
+                    sv[((size_t)z * res + y) * res + x] = v;
+                }
+        double off = o.exOff;
+        auto& den = h.getDensity();
+        jet::FmmLevelSetSolver3 fmm;
+        fmm.extrapolate<REAL, CellCenteredScalarGrid3Ptr>(den, sdf, o.exMax, den, nullptr,
+                                                          [off](REAL d, REAL v) { return v < -off * d; });
+        Archive ex;
+        ex.f64("sdf", sv);
+        std::vector<double> dO, dT;
+        for (int l = 0; l < h.levels(); ++l) {
+            for (double v : den->getOctagonGrid()->getData()[l]) dO.push_back(v);
+            for (double v : den->getTiltGrid()->getData()[l]) dT.push_back(v);
+        }
+        ex.f64("density_oct", dO);
+        ex.f64("density_tilt", dT);
+        ex.write(o.out + "/extrap.astg");
+    }
     return 0;
 }

@@ -29,6 +29,8 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <queue>
+#include <tuple>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -1906,6 +1908,216 @@ public:
         halfMark.assign(S, 0);
         for (int hs : halfTilts) halfMark[hs] = 1;
     }
+
+    // ---------------------------------------------------------------- extrapolation
+    // CellCenteredGrid<REAL,3>::sample (include/cell_centered_grid.h:40-54) on a res^3 signed
+    // distance grid of spacing 1/res (index (z*res + y)*res + x)
+    double sdfSample(const std::vector<double>& sdf, int sres, const V3& p) const {
+        double sd = 1.0 / sres;
+        double rp[3] = {p.x / sd - 0.5, p.y / sd - 0.5, p.z / sd - 0.5};
+        int i[3], i1[3];
+        double f[3];
+        for (int k = 0; k < 3; ++k) {
+            bary_vec(rp[k], sres - 1, &i[k], &f[k]);
+            i1[k] = std::min(i[k] + 1, sres - 1);
+        }
+        auto g = [&](int x, int y, int z) { return sdf[((size_t)z * sres + y) * sres + x]; };
+        return trilerp(g(i[0], i[1], i[2]), g(i1[0], i[1], i[2]), g(i[0], i1[1], i[2]), g(i1[0], i1[1], i[2]),
+                       g(i[0], i[1], i1[2]), g(i1[0], i[1], i1[2]), g(i[0], i1[1], i1[2]), g(i1[0], i1[1], i1[2]),
+                       f[0], f[1], f[2]);
+    }
+    // FmmLevelSetSolver3::extrapolate (include/jet/fmm_levelset_solver3.h:84-408) with no cached
+    // marker: the scalar omni field (oct, til) of the current buffer is extrapolated in place
+    // from the nodes where sdf < -offset * d (d: dx_l sqrt(3)/2 for octagons, e for tilts, dx_l
+    // for half tilts) outward, in increasing order of the SDF sampled at each node, up to
+    // maxFactor * dx_0.  Sequential: the reference gathers its first candidates per worker slice
+    // in slice order, which is this node order.  Returns the number of nodes assigned.
+    enum { K_UNKNOWN = 0, K_KNOWN = 1, K_TRIAL = 2, K_DONT_TOUCH = 3, K_GHOST = 4 };
+    enum { M_TILT = 0, M_OCT = 1, M_HALF = 2 };
+    long long extrapolate(std::vector<double>& oct, std::vector<double>& til, const std::vector<double>& sdf, int sres,
+                          double offset, double maxFactor) {
+        const std::vector<TiltE>& te = tiltE[cur];
+        auto valid = [&](double d, double v) { return v < -offset * d; };
+        std::vector<char> mO(S, K_UNKNOWN), mT(S, K_UNKNOWN);
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & F_GHOST) continue;
+            int l = slev[s];
+            if (octValid(l, sx[s], sy[s], sz[s])) {
+                if (valid(dh(l) * SQRT3 * 0.5, sdfSample(sdf, sres, cellPos(s)))) mO[s] = K_KNOWN;
+            } else {
+                mO[s] = K_DONT_TOUCH;
+            }
+        }
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & F_GHOST) continue;
+            if (te[s].closed) mT[s] = K_DONT_TOUCH;
+            else if (valid(te[s].e, sdfSample(sdf, sres, vertPos(s)))) mT[s] = K_KNOWN;
+        }
+        for (int s = 0; s < S; ++s)
+            if (sflag[s] & F_GHOST) { mO[s] = K_GHOST; mT[s] = K_GHOST; }
+        for (int hs : halfTilts)
+            if (valid(dh(slev[hs]), sdfSample(sdf, sres, vertPos(hs)))) mT[hs] = K_KNOWN;
+
+        typedef std::tuple<char, int, double> Item;
+        auto cmp = [](const Item& a, const Item& b) { return std::get<2>(a) * 1.0 > std::get<2>(b) * 1.0; };
+        std::vector<Item> arr;
+        auto sdfO = [&](int t) { return sdfSample(sdf, sres, cellPos(t)); };
+        auto sdfT = [&](int t) { return sdfSample(sdf, sres, vertPos(t)); };
+        // a tilt vertex that is a ghost stands for the non-ghost node getUntil finds, when that
+        // node is finer or sits at the same corner (the reference's test, :176-178 and :322-325)
+        auto ghostTilt = [&](int l, int x, int y, int z) {
+            int c0 = getUntil(l, x, y, z, true);
+            if (c0 < 0) c0 = getUntil(l, x, y, z, false);
+            if (c0 < 0) return -1;
+            if (slev[c0] < l || ((sx[c0] << 1) == x && (sy[c0] << 1) == y && (sz[c0] << 1) == z)) return c0;
+            return -1;
+        };
+        auto halfNb = [&](int hs, int out[8]) {  // halfTiltNeighborOctagon3 + the big octagon
+            const TiltE& n = te[hs];
+            int l = slev[hs], x = sx[hs], y = sy[hs], z = sz[hs];
+            for (int k = 0; k < 8; ++k) out[k] = -1;
+            for (int i = 0; i < 4; ++i) {
+                int k = HALF_SLOT[n.dir][i];
+                out[k] = slotOf(l, x + TILT_NB_OCT[k][0], y + TILT_NB_OCT[k][1], z + TILT_NB_OCT[k][2]);
+            }
+            int id[3] = {x >> 1, y >> 1, z >> 1};
+            id[n.dir % 3] -= n.dir < 3 ? 1 : 0;
+            out[HALF_SLOT[n.dir][4]] = (l + 1 < L) ? slotOf(l + 1, id[0], id[1], id[2]) : -1;
+        };
+        auto tiltNbSlots = [&](int s, int out[8]) {  // tiltNeighborOctagon3 as slots (-1: none)
+            NbOct nb[8];
+            tiltNbOct(slev[s], sx[s], sy[s], sz[s], nb);
+            for (int k = 0; k < 8; ++k) out[k] = nb[k].some ? slotOf(nb[k].l, nb[k].x, nb[k].y, nb[k].z) : -1;
+        };
+        // first ring (:154-205), node order
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & F_GHOST) continue;
+            int l = slev[s], x = sx[s], y = sy[s], z = sz[s];
+            if (mO[s] == K_KNOWN) {
+                for (int k = 0; k < 6; ++k) {
+                    int tx = x + OCT_NB[k][0], ty = y + OCT_NB[k][1], tz = z + OCT_NB[k][2];
+                    if (!octValid(l, tx, ty, tz)) continue;
+                    int t = slotOf(l, tx, ty, tz);
+                    if (t >= 0 && mO[t] == K_UNKNOWN) { mO[t] = K_TRIAL; arr.emplace_back(M_OCT, t, sdfO(t)); }
+                }
+                if (l >= 1) {
+                    for (int k = 0; k < 6; ++k) {
+                        int axis = k >> 1;
+                        int id[3] = {2 * x + 1, 2 * y + 1, 2 * z + 1};
+                        id[axis] += (k & 1) ? 1 : -1;
+                        int t = slotOf(l - 1, id[0], id[1], id[2]);
+                        if (t >= 0 && te[t].half && mT[t] == K_UNKNOWN) { mT[t] = K_TRIAL; arr.emplace_back(M_HALF, t, sdfT(t)); }
+                    }
+                }
+                for (int k = 0; k < 8; ++k) {
+                    int tx = x + OCT_NB_TILT[k][0], ty = y + OCT_NB_TILT[k][1], tz = z + OCT_NB_TILT[k][2];
+                    int t = slotOf(l, tx, ty, tz);
+                    if (t < 0) continue;
+                    if (mT[t] == K_UNKNOWN) {
+                        mT[t] = K_TRIAL;
+                        arr.emplace_back(te[t].half ? M_HALF : M_TILT, t, sdfT(t));
+                    } else if (mT[t] == K_GHOST) {
+                        int c0 = ghostTilt(l, tx, ty, tz);
+                        if (c0 >= 0 && mT[c0] == K_UNKNOWN) {
+                            mT[c0] = K_TRIAL;
+                            arr.emplace_back(te[c0].half ? M_HALF : M_TILT, c0, sdfT(c0));
+                        }
+                    }
+                }
+            }
+            if (mT[s] == K_KNOWN && !te[s].half) {
+                int nb[8];
+                tiltNbSlots(s, nb);
+                for (int k = 0; k < 8; ++k) {
+                    int t = nb[k];
+                    if (t >= 0 && mO[t] == K_UNKNOWN) { mO[t] = K_TRIAL; arr.emplace_back(M_OCT, t, sdfO(t)); }
+                }
+            }
+        }
+        for (int hs : halfTilts) {
+            if (mT[hs] != K_KNOWN) continue;
+            int nb[8];
+            halfNb(hs, nb);
+            for (int k = 0; k < 8; ++k) {
+                int t = nb[k];
+                if (t >= 0 && mO[t] == K_UNKNOWN) { mO[t] = K_TRIAL; arr.emplace_back(M_OCT, t, sdfO(t)); }
+            }
+        }
+        std::priority_queue<Item, std::vector<Item>, decltype(cmp)> heap{cmp, std::move(arr)};
+        // propagation (:257-405)
+        long long assigned = 0;
+        const double limit = dh(0) * maxFactor;
+        while (!heap.empty()) {
+            Item it = heap.top();
+            heap.pop();
+            int mark = std::get<0>(it), c = std::get<1>(it);
+            if (std::fabs(std::get<2>(it)) > limit) break;
+            if ((mark == M_OCT ? mO[c] : mT[c]) == K_KNOWN) continue;
+            int l = slev[c], x = sx[c], y = sy[c], z = sz[c];
+            double sum = 0.0, count = 0.0;
+            if (mark == M_TILT) {
+                int nb[8];
+                tiltNbSlots(c, nb);
+                for (int k = 0; k < 8; ++k) {
+                    int t = nb[k];
+                    if (t < 0) continue;
+                    if (mO[t] == K_KNOWN) { sum += oct[t]; count += 1; }
+                    else if (mO[t] == K_UNKNOWN) { mO[t] = K_TRIAL; heap.push(Item(M_OCT, t, sdfO(t))); }
+                }
+            } else if (mark == M_OCT) {
+                for (int k = 0; k < 6; ++k) {
+                    int tx = x + OCT_NB[k][0], ty = y + OCT_NB[k][1], tz = z + OCT_NB[k][2];
+                    if (!octValid(l, tx, ty, tz)) continue;
+                    int t = slotOf(l, tx, ty, tz);
+                    if (t < 0) continue;
+                    if (mO[t] == K_KNOWN) { sum += oct[t]; count += 1; }
+                    else if (mO[t] == K_UNKNOWN) { mO[t] = K_TRIAL; heap.push(Item(M_OCT, t, sdfO(t))); }
+                }
+                if (l >= 1) {
+                    for (int k = 0; k < 6; ++k) {
+                        int axis = k / 2;
+                        int id[3] = {2 * x + 1, 2 * y + 1, 2 * z + 1};
+                        id[axis] += (k & 1) ? 1 : -1;
+                        int t = slotOf(l - 1, id[0], id[1], id[2]);
+                        if (t < 0 || !te[t].half) continue;
+                        if (mT[t] == K_KNOWN) { sum += til[t]; count += 1; }
+                        else if (mT[t] == K_UNKNOWN) { mT[t] = K_TRIAL; heap.push(Item(M_HALF, t, sdfT(t))); }
+                    }
+                }
+                for (int k = 0; k < 8; ++k) {
+                    int tx = x + OCT_NB_TILT[k][0], ty = y + OCT_NB_TILT[k][1], tz = z + OCT_NB_TILT[k][2];
+                    int t = slotOf(l, tx, ty, tz);
+                    if (t < 0) continue;
+                    if (mT[t] == K_KNOWN) { sum += til[t]; count += 1; }
+                    else if (mT[t] == K_UNKNOWN) {
+                        mT[t] = K_TRIAL;
+                        heap.push(Item(te[t].half ? M_HALF : M_TILT, t, sdfT(t)));
+                    } else if (mT[t] == K_GHOST) {
+                        int c0 = ghostTilt(l, tx, ty, tz);
+                        if (c0 < 0) continue;
+                        if (mT[c0] == K_KNOWN) { sum += til[t]; count += 1; }  // the ghost slot's own value
+                        else if (mT[c0] == K_UNKNOWN) {
+                            mT[c0] = K_TRIAL;
+                            heap.push(Item(te[c0].half ? M_HALF : M_TILT, c0, sdfT(c0)));
+                        }
+                    }
+                }
+            } else {
+                int nb[8];
+                halfNb(c, nb);
+                for (int k = 0; k < 8; ++k) {
+                    int t = nb[k];
+                    if (t < 0) continue;
+                    if (mO[t] == K_KNOWN) { sum += oct[t]; count += 1; }
+                    else { mO[t] = K_TRIAL; heap.push(Item(M_OCT, t, sdfO(t))); }
+                }
+            }
+            if (mark == M_OCT) { oct[c] = sum / count; mO[c] = K_KNOWN; }
+            else { til[c] = sum / count; mT[c] = K_KNOWN; }
+            ++assigned;
+        }
+        return assigned;
+    }
 };
 
 }  // namespace oracle
@@ -2138,6 +2350,18 @@ int orc_solve(void* h, int n, const int* rowptr, const int* col, const double* v
     s->P.maxIter = saveIt;
     memcpy(x, s->p.data(), sizeof(double) * n);
     return s->pcgIters;
+}
+
+// FmmLevelSetSolver3::extrapolate of "density" or "heat" (current buffer), in place; returns the
+// number of nodes assigned, -1 on a bad argument
+long long orc_extrapolate(void* h, const char* field, const double* sdf, int sres, double offset, double maxFactor) {
+    auto* s = (oracle::Solver*)h;
+    std::string f = field ? field : "";
+    if ((f != "density" && f != "heat") || !sdf || sres <= 1) return -1;
+    std::vector<double> g(sdf, sdf + (size_t)sres * sres * sres);
+    int c = s->cur;
+    if (f == "density") return s->extrapolate(s->dO[c], s->dT[c], g, sres, offset, maxFactor);
+    return s->extrapolate(s->hO[c], s->hT[c], g, sres, offset, maxFactor);
 }
 
 int orc_size(void* h, int what) {

@@ -12,6 +12,13 @@ Fixture keys (all arrays in the reference's slot order, see oracle/smoke_oracle.
   per step k (1-based) final state: step<k>/<field>, step<k>/t_<field>, and the projection of
           that step: step<k>/A_rowptr, A_col, A_val, b, p, pcg_iters, pindex_oct, pindex_tilt, ambT
   stage snapshots of step 1 (when recorded): stage1_<name>/<field>, t_<field>
+
+Extrapolation fixtures (ref_extrap_*.npz): the state after the steps (before/<field>), the sphere
+signed distance grid the harness built (sdf, res^3), the density after the reference's
+FmmLevelSetSolver3::extrapolate (after/density_oct, after/density_tilt), meta/case and
+meta/extrap = [cx, cy, cz, r, max_distance_factor, offset].
+
+    python tests/golden/make_golden.py --extrap-only
 """
 import os
 import subprocess
@@ -31,6 +38,33 @@ CASES = [
     ("ref_c16_l2", 16, 2, 3, False),
 ]
 STAGES = ["scene", "force", "preproject", "project", "dual", "advect"]
+EXTRAP_CASES = [
+    # name, coarsest, levels, steps, (centre x, y, z, radius, max distance factor, validity offset)
+    ("ref_extrap_c8_l3", 8, 3, 2, (0.47, 0.53, 0.29, 0.15, 4.0, 0.0)),
+    ("ref_extrap_c16_l2", 16, 2, 2, (0.52, 0.44, 0.21, 0.11, 6.0, 0.5)),
+]
+
+
+def extrap_fixtures(harness):
+    for name, c, lv, steps, ex in EXTRAP_CASES:
+        with tempfile.TemporaryDirectory() as d:
+            cmd = [harness, "--coarsest", str(c), "--levels", str(lv), "--steps", str(steps), "--out", d,
+                   "--extrapolate", ",".join(repr(v) for v in ex)]
+            subprocess.check_call(cmd)
+            out = {}
+            st = astg_archive.read(os.path.join(d, f"step_{steps:04d}.astg"))
+            for key, v in st.items():
+                if key != "wall_s":
+                    out[f"before/{key}"] = v
+            exr = astg_archive.read(os.path.join(d, "extrap.astg"))
+            out["sdf"] = exr["sdf"]
+            out["after/density_oct"] = exr["density_oct"]
+            out["after/density_tilt"] = exr["density_tilt"]
+            out["meta/case"] = np.array([c, lv, steps], dtype=np.int32)
+            out["meta/extrap"] = np.array(ex, dtype=np.float64)
+            path = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(path, **out)
+            print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB, {len(out)} arrays")
 
 
 def main():
@@ -38,6 +72,9 @@ def main():
     subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref", "Makefile"), f"REF={ref}",
                            "-j8"])
     harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+    extrap_fixtures(harness)
+    if "--extrap-only" in sys.argv:
+        return
     for name, c, lv, steps, stages in CASES:
         with tempfile.TemporaryDirectory() as d:
             cmd = [harness, "--coarsest", str(c), "--levels", str(lv), "--steps", str(steps), "--out", d]

@@ -86,3 +86,22 @@ def test_standalone_pcg_reproduces_reference_solution(name):
         x, it = o.solve(st["A_rowptr"], st["A_col"], st["A_val"], st["b"])
         assert it == int(st["pcg_iters"][0])
         assert_same(f"step{k}/p", st["p"], x)
+
+
+@pytest.mark.parametrize("name", ["ref_extrap_c8_l3", "ref_extrap_c16_l2"])
+def test_extrapolation_bit_exact(name):
+    """FmmLevelSetSolver3::extrapolate (include/jet/fmm_levelset_solver3.h:84-408) on the
+    reference's own state: the oracle's heap march assigns the same values bit for bit."""
+    g = golden(name)
+    c, lv, _ = g["meta/case"].tolist()
+    cx, cy, cz, r, maxf, off = g["meta/extrap"].tolist()
+    o = Oracle(c, lv)
+    before = state(g, "before/")
+    for k in FIELDS:
+        o.set(k, before[k])
+    n = o.extrapolate("density", g["sdf"], off, maxf)
+    assert n > 100
+    assert_same("after/density_oct", g["after/density_oct"], o.get("density_oct"))
+    assert_same("after/density_tilt", g["after/density_tilt"], o.get("density_tilt"))
+    changed = np.sum(g["after/density_oct"] != before["density_oct"]) + np.sum(g["after/density_tilt"] != before["density_tilt"])
+    assert changed > 50
