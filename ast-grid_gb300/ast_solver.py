@@ -22,13 +22,17 @@ FP64, MIXED = 0, 1
 # exported symbols of include/astg.h
 SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_stage",
            "astg_set_solver_parameters", "astg_set_precision", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
-           "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc"]
+           "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate"]
 
 
 class AstgError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"{STATUS.get(status, status)}: {message}")
         self.status = status
+
+
+class ExtrapStats(ctypes.Structure):
+    _fields_ = [("assigned", ctypes.c_longlong), ("passes", ctypes.c_int), ("ms", ctypes.c_double)]
 
 
 class Params(ctypes.Structure):
@@ -82,6 +86,8 @@ def lib(path=None):
         L.astg_solve.argtypes = [c_p, ctypes.c_int, c_p, c_p, c_p, c_p, c_p, ctypes.c_double, ctypes.c_int,
                                  ctypes.c_int, ctypes.POINTER(SolveStats)]
         L.astg_max_velocity.argtypes = [c_p, ctypes.POINTER(ctypes.c_double)]
+        L.astg_extrapolate.argtypes = [c_p, ctypes.c_char_p, c_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                       ctypes.POINTER(ExtrapStats)]
         L.astg_mean_temperature_noalloc.argtypes = [c_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int, c_p, c_p,
                                                     ctypes.c_char_p, ctypes.c_size_t]
         _lib = L
@@ -243,6 +249,18 @@ class OctreeSmoke3:
                                      x.ctypes.data, rel_tol, max_iter, prec, ctypes.byref(st)),
                     allow=(ASTG_NOT_CONVERGED,))
         return x, st
+
+    def extrapolate(self, field, sdf, valid_offset=0.0, max_distance_factor=4.0):
+        """FmmLevelSetSolver3::extrapolate (include/jet/fmm_levelset_solver3.h:84-408) of "density"
+        or "heat" in place; sdf is res^3 (index (z*res + y)*res + x).  Returns ExtrapStats."""
+        g = np.ascontiguousarray(sdf, dtype=np.float64).ravel()
+        res = round(len(g) ** (1.0 / 3.0))
+        if res ** 3 != len(g):
+            raise ValueError("sdf must hold res^3 values")
+        st = ExtrapStats()
+        self._check(lib().astg_extrapolate(self._h, field.encode(), g.ctypes.data, res, valid_offset,
+                                           max_distance_factor, ctypes.byref(st)))
+        return st
 
     def max_velocity(self):
         v = ctypes.c_double()

@@ -743,6 +743,41 @@ struct astg_handle {
         readSolveStats();
     }
 
+    // FmmLevelSetSolver3::extrapolate of "density" or "heat" (current buffer), in place
+    double* exSdf = nullptr;
+    size_t exSdfCap = 0;
+    void* exScratch = nullptr;
+    void extrapolate(const std::string& field, const double* sdf, int sres, double offset, double maxFactor,
+                     astg_extrap_stats* stats) {
+        if (field != "density" && field != "heat") throw std::invalid_argument("astg_extrapolate: field must be density or heat");
+        if (sres < 2 || sres > 4096) throw std::invalid_argument("astg_extrapolate: sdf_res must be 2..4096");
+        if (!(maxFactor >= 0) || !(offset == offset)) throw std::invalid_argument("astg_extrapolate: bad distance arguments");
+        size_t n = (size_t)sres * sres * sres;
+        if (n > exSdfCap) {
+            exSdf = dalloc<double>(n);
+            exSdfCap = n;
+        }
+        if (!exScratch) exScratch = dalloc<char>(extrapolate_scratch_bytes(S));
+        ck(cudaMemcpyAsync(exSdf, sdf, n * sizeof(double), cudaMemcpyHostToDevice, st), "upload sdf");
+        Fields& C = F[cur];
+        double* oct = field == "density" ? C.dO : C.hO;
+        double* til = field == "density" ? C.dT : C.hT;
+        ck(cudaEventRecord(evA, st), "event");
+        int passes = 0;
+        long long got = launch_extrapolate(d, C, oct, til, exSdf, sres, offset, maxFactor, exScratch, &passes, st);
+        ck(cudaEventRecord(evB, st), "event");
+        ck(cudaStreamSynchronize(st), "extrapolate");
+        if (got < 0) ck(cudaGetLastError(), "extrapolate");
+        checkStatus();
+        if (stats) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, evA, evB);
+            stats->assigned = got;
+            stats->passes = passes;
+            stats->ms = ms;
+        }
+    }
+
     void readSolveStats() {
         int isc[ISC_COUNT], n = 0, nnz = 0;
         double sc[SC_COUNT];
@@ -1195,6 +1230,12 @@ astg_status astg_max_velocity(astg_handle* h, double* out) {
         for (double v : mac) m = std::max(m, v);
         *out = m;
     });
+}
+
+astg_status astg_extrapolate(astg_handle* h, const char* field, const double* sdf, int sdf_res, double valid_offset,
+                             double max_distance_factor, astg_extrap_stats* stats) {
+    if (!h || !field || !sdf) return ASTG_BAD_ARG;
+    return guard(h, [&] { h->extrapolate(field, sdf, sdf_res, valid_offset, max_distance_factor, stats); });
 }
 
 // Takes no handle and allocates nothing, on the device or the host: the chunk partials go to a

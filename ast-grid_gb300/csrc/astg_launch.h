@@ -177,5 +177,10 @@ void launch_advect_scalars(const Dev& d, const Fields& cur, const Fields& nxt, c
                            cudaStream_t st);
 void launch_advect_velocity(const Dev& d, const Fields& cur, const Fields& nxt, double dt, cudaStream_t st);
 void launch_decay(const Dev& d, const Fields& F, cudaStream_t st);
+// FmmLevelSetSolver3::extrapolate of (oct, til) in place from a res^3 signed distance grid on the
+// device; scratch holds extrapolate_scratch_bytes(S); returns the nodes assigned (-1: CUDA error)
+size_t extrapolate_scratch_bytes(int S);
+long long launch_extrapolate(const Dev& d, const Fields& F, double* oct, double* til, const double* sdf, int sres,
+                             double offset, double maxFactor, void* scratch, int* passes, cudaStream_t st);
 
 }  // namespace astg

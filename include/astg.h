@@ -144,6 +144,23 @@ astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32
  * (src/octree_omnigrid_solver3.cpp:1066-1122). */
 astg_status astg_max_velocity(astg_handle* h, double* out);
 
+typedef struct astg_extrap_stats {
+    long long assigned;   /* nodes given an extrapolated value */
+    int passes;           /* parallel passes (dependency rounds) used */
+    double ms;            /* device time (CUDA events) */
+} astg_extrap_stats;
+
+/* FmmLevelSetSolver3::extrapolate (include/jet/fmm_levelset_solver3.h:84-408) with no cached
+ * marker, in place on the scalar omni field `field` ("density" or "heat": octagon and tilt values
+ * of the current state).  sdf is a signed distance grid of sdf_res^3 cell-centred values on the
+ * unit cube (index (z*res + y)*res + x), sampled trilinearly like CellCenteredGrid::sample.  Nodes
+ * whose sample v satisfies v < -valid_offset * d are known (d: dx_l*sqrt(3)/2 for octagons, the
+ * tilt size e for tilts, dx_l for half tilts); the others are filled outward in increasing SDF
+ * order with the mean of their known neighbours, up to max_distance_factor * dx_0 (the finest
+ * spacing).  Ghost values are left as they are, as in the reference. */
+astg_status astg_extrapolate(astg_handle* h, const char* field, const double* sdf, int sdf_res, double valid_offset,
+                             double max_distance_factor, astg_extrap_stats* stats);
+
 /* Mean temperature ambT of addForce (src/octree_omnigrid_solver3.cpp:922-929) over an octagon heat
  * array the caller keeps in its own device memory.  It is the reduction astg_step runs in its force
  * stage, with the same fixed summation tree, so the result equals astg_get(h, "ambT") bit for bit
