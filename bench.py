@@ -173,6 +173,68 @@ def cpu_baseline_sample(steps):
                       f"bit-identical to the reference's CPU algorithm), {el:.1f} s"}
 
 
+def isolated_solves(args, device):
+    """Isolated pressure solves: the octree and tilt state frozen after `solve_steps` steps of the
+    scene; each right-hand side is the AST divergence (the projection's own assembly) of face and
+    tilted-face velocities drawn i.i.d. N(0,1) with a fixed seed, smoothed by 3 weighted Jacobi
+    passes (omega 2/3 on A, include/pcgsolver/pcg_solver.h:276-300), then solved to |r| <= 1e-6 |b|
+    in FP64 and in mixed precision.  ms excludes the MIC(0) factorisation."""
+    import numpy as np
+
+    import ast_solver
+
+    s = ast_solver.OctreeSmoke3(COARSEST, LEVELS, device=device)
+    for _ in range(args.solve_steps):
+        s.update(DT)
+    fields = ["density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
+              "tilt_e", "tilt_flags"]
+    snap = {k: s.get(k) for k in fields + ["t_" + k for k in fields] + ["tilt_open"]}
+    S = s.slots
+    out = {"fp64": [], "mixed": []}
+    A = None
+    for k in range(args.solve_rhs):
+        rng = np.random.default_rng(1 + k)
+        s.set("mac", rng.standard_normal(3 * S))
+        s.set("tilt_vel", rng.standard_normal(8 * S))
+        s.stage(3, DT)  # assembles A and b = div(u) for the frozen state
+        b = s.get("b")
+        if A is None:
+            A = (s.get("A_rowptr"), s.get("A_col"), s.get("A_val"))
+        for kk, v in snap.items():
+            s.set(kk, v)
+        rp, col, val = A
+        n = len(rp) - 1
+        diag = np.zeros(n)
+        rows = np.repeat(np.arange(n), np.diff(rp))
+        on = col == rows
+        diag[rows[on]] = val[on]
+        for _ in range(3):
+            ax = np.add.reduceat(val * b[col], rp[:-1])
+            b = (1 - 2 / 3.0) * b + (2 / 3.0) * (0.0 - (ax - diag * b)) / diag
+        for prec in ("fp64", "mixed"):
+            _, st = s.solve(rp, col, val, b, rel_tol=1e-6, precision=prec)
+            out[prec].append((st.ms, st.iterations, st.outer, st.converged))
+    rp, col, val = A
+    n, nnz = len(rp) - 1, len(col)
+    nnzL = (nnz - n) / 2
+    res = {"config": f"{args.solve_rhs} right-hand sides on the octree frozen after {args.solve_steps} steps, "
+                     "div of N(0,1) faces smoothed by 3 weighted Jacobi passes, rel. residual 1e-6",
+           "n": n, "nnz": nnz}
+    for prec, rows_ in out.items():
+        ms = float(np.mean([r[0] for r in rows_]))
+        it = float(np.mean([r[1] for r in rows_]))
+        outer = float(np.mean([r[2] for r in rows_]))
+        if prec == "fp64":
+            bytes_ = it * (12 * nnz + 24 * nnzL + 180 * n)
+        else:
+            bytes_ = it * (8 * nnz + 16 * nnzL + 96 * n) + outer * (12 * nnz + 28 * n)
+        res[prec] = {"ms_per_solve": ms, "iterations_mean": it, "outer_cycles_mean": outer,
+                     "all_converged": all(r[3] == 1 for r in rows_), "algorithmic_GBps": bytes_ / (ms / 1e3) / 1e9}
+    res["mixed_speedup"] = res["fp64"]["ms_per_solve"] / res["mixed"]["ms_per_solve"]
+    s.close()
+    return res
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if ws > 1 and rank != 0:
@@ -333,6 +395,9 @@ def run_ours(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(args.cpu_steps)
+    solves = None
+    if rank == 0 and args.solve_rhs > 0:
+        solves = isolated_solves(args, local)
 
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
@@ -343,7 +408,7 @@ def run_ours(args):
             "pcg_ms_per_solve": float(np.mean(pcg_ms)), "pcg_iters_mean": float(np.mean(iters)), "mixed": mixed,
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "roofline": roofline, "kernels": kernel_breakdown, "cpu_baseline": cpu, "e2e": e2e,
-            "clocks": clocks, "gpu_launches": launches}
+            "clocks": clocks, "gpu_launches": launches, "isolated_solves": solves}
     s.close()
     D.barrier()
     if rank == 0:
@@ -361,6 +426,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10, help="steps of the end-to-end loop")
+    ap.add_argument("--solve-steps", type=int, default=100, help="steps before the isolated solves")
+    ap.add_argument("--solve-rhs", type=int, default=20, help="right-hand sides of the isolated solves (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
