@@ -941,15 +941,15 @@ template <typename T> struct Pca;
 template <> struct Pca<double> {
     typedef unsigned long long Bits;
     static constexpr Bits EMPTY = 0x7FF4DEADBEEF0001ull;
-    // Polls are plain (weak) shared-memory loads kept in place by asm volatile: shared memory is
-    // not cached, so each one reads the slot's current contents, and an aligned store is seen
+    // Polls are plain (weak) loads of shared-memory slots kept in place by asm volatile: shared
+    // memory is not cached, so each one reads the slot's current contents, and an aligned store is seen
     // whole or not at all.  The value itself is the signal, so nothing else needs ordering; the
     // cluster barrier at the end of each sweep orders everything for what follows.  (Loads with
     // .relaxed.cluster semantics measured about 20x slower per polling pass with every warp of
     // the cluster polling.)
-    static __device__ __forceinline__ Bits ld(uint32_t a) {
+    static __device__ __forceinline__ Bits ld(const void* a) {
         Bits v;
-        asm volatile("ld.shared::cluster.b64 %0, [%1];" : "=l"(v) : "r"(a) : "memory");
+        asm volatile("ld.b64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
         return v;
     }
     static __device__ __forceinline__ void st(uint32_t a, double v) {
@@ -960,9 +960,9 @@ template <> struct Pca<double> {
 template <> struct Pca<float> {
     typedef unsigned int Bits;
     static constexpr Bits EMPTY = 0x7FA5DEADu;
-    static __device__ __forceinline__ Bits ld(uint32_t a) {
+    static __device__ __forceinline__ Bits ld(const void* a) {
         Bits v;
-        asm volatile("ld.shared::cluster.b32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+        asm volatile("ld.b32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
         return v;
     }
     static __device__ __forceinline__ void st(uint32_t a, float v) {
@@ -1010,32 +1010,34 @@ __device__ __forceinline__ void pca_load(const Proj& P, const PcaData<T>& D, int
 // One row per lane; the warp polls until every lane's row is done.  A lane stores its row the
 // moment its last entry arrives, so no lane ever waits for a lane of its own warp while holding its
 // own result back.  The loop and its exit are warp-uniform.  Entry addresses are resolved once per
-// row into the cluster's shared-memory window (mapa), so every poll is one load form for local
-// and remote entries alike; every pass re-loads all entries still missing, so they resolve in
-// parallel.  Bounded: after PCA_SPIN_LIMIT polls (or once any wait of the launch has given up) the
-// warp stops waiting and reports.
-__device__ __forceinline__ uint32_t pca_window(uint32_t own, int packed, uint32_t esize) {
-    uint32_t a = own + (uint32_t)(packed & 0xffffff) * esize, m;
-    asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(m) : "r"(a), "r"((uint32_t)(packed >> 24)));
-    return m;
-}
+// row into generic addresses: a slot of the CTA's own shared memory is read there directly, a slot
+// of another CTA through the cluster's distributed shared memory, with one load form for both
+// (measured 2-3 % faster than routing every entry through the cluster window); every pass
+// re-loads all entries still missing, so they resolve in parallel.  Bounded: after PCA_SPIN_LIMIT
+// polls (or once any wait of the launch has given up) the warp stops waiting and reports.
 constexpr int PCA_MAXE = 2 * PC_MAXE;  // entries a row resolves in registers (8 from the record)
 // The polling pass is integer-only: it re-loads the entries not yet known to hold values and
 // extends the prefix of present ones.  The arithmetic runs once per row, after every entry is
 // present, in the reference's order (FP64 issue is scarce on this part, and predicated-off FP64
 // instructions in a polling pass would still occupy the FP64 pipe on every pass).
+// generic address of packed entry (owner << 24 | local): the CTA's own slots resolve to its shared
+// memory, other CTAs' slots to the cluster's distributed shared memory
+template <typename T>
+__device__ __forceinline__ const T* pca_gptr(T* const* win, int packed) {
+    return win[packed >> 24] + (packed & 0xffffff);
+}
 template <typename T>
 __device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaData<T>& D, const PcaRow<T>& w, bool fwd,
-                                              uint32_t own, int* status) {
+                                              uint32_t own, T* const* win, int* status) {
     typedef Pca<T> K;
     typedef typename K::Bits Bits;
     const uint32_t es = sizeof(T);
     bool done = w.cnt < 0;
-    uint32_t a[PCA_MAXE];
+    const T* a[PCA_MAXE];
     T val[PCA_MAXE];
 #pragma unroll
     for (int e = 0; e < PC_MAXE; ++e) {
-        a[e] = pca_window(own, w.col[e], es);
+        a[e] = pca_gptr(win, w.col[e]);
         val[e] = w.val[e];
     }
     // entries 8..15 of a longer row: loaded once, together, before any polling
@@ -1045,7 +1047,7 @@ __device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaData<T>& D
 #pragma unroll
     for (int e = PC_MAXE; e < PCA_MAXE; ++e) {
         bool has = e < w.cnt;
-        a[e] = pca_window(own, has ? oc[q0 + e] : 0, es);
+        a[e] = pca_gptr(win, has ? oc[q0 + e] : 0);
         val[e] = has ? ov[q0 + e] : T(0);
     }
     const int lim = min(w.cnt, PCA_MAXE);
@@ -1074,7 +1076,7 @@ __device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaData<T>& D
             }
             // rows longer than PCA_MAXE entries: the rest one at a time from the compact arrays
             while (part && got < w.cnt) {
-                Bits x = K::ld(pca_window(own, oc[q0 + got], es));
+                Bits x = K::ld(pca_gptr(win, oc[q0 + got]));
                 if (x == K::EMPTY) break;
                 acc = acc - ov[q0 + got] * K::val(x);
                 ++got;
@@ -1108,6 +1110,9 @@ __global__ void __launch_bounds__(PCA_THREADS, 1) k_precond_async(Proj P, PcaDat
     const int rows = P.ownStart[rank + 1] - base;
     const int lgB = P.pcLgBlock;
     const uint32_t own = (uint32_t)__cvta_generic_to_shared(pca_smem);
+    __shared__ T* win[16];
+    if (threadIdx.x < cl.num_blocks()) win[threadIdx.x] = cl.map_shared_rank(zsh, (int)threadIdx.x);
+    if (threadIdx.x == rank) win[threadIdx.x] = zsh;
     for (int l = threadIdx.x; l < chunk; l += blockDim.x) zraw[l] = K::EMPTY;
     cl.sync();  // every CTA is running and every slot of the cluster is empty
     for (int dir = 0; dir < 2; ++dir) {
@@ -1127,7 +1132,7 @@ __global__ void __launch_bounds__(PCA_THREADS, 1) k_precond_async(Proj P, PcaDat
         pca_load(P, D, base, pick(0), rows, fwd, W);
         for (int k = 0; k < rounds; ++k) {
             pca_load(P, D, base, pick(k + 1), rows, fwd, X);
-            pca_solve_row(P, D, W, fwd, own, status);
+            pca_solve_row(P, D, W, fwd, own, win, status);
             W = X;
         }
         cl.sync();  // sweep finished everywhere (global and shared writes ordered at cluster scope)
