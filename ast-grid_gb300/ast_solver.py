@@ -22,7 +22,8 @@ FP64, MIXED = 0, 1
 # exported symbols of include/astg.h
 SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_stage",
            "astg_set_solver_parameters", "astg_set_precision", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
-           "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate"]
+           "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate",
+           "astg_restart", "astg_save_checkpoint"]
 
 
 class AstgError(RuntimeError):
@@ -86,6 +87,8 @@ def lib(path=None):
         L.astg_solve.argtypes = [c_p, ctypes.c_int, c_p, c_p, c_p, c_p, c_p, ctypes.c_double, ctypes.c_int,
                                  ctypes.c_int, ctypes.POINTER(SolveStats)]
         L.astg_max_velocity.argtypes = [c_p, ctypes.POINTER(ctypes.c_double)]
+        L.astg_restart.argtypes = [c_p, ctypes.c_int] + [ctypes.c_char_p] * 6
+        L.astg_save_checkpoint.argtypes = [c_p] + [ctypes.c_char_p] * 5
         L.astg_extrapolate.argtypes = [c_p, ctypes.c_char_p, c_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                        ctypes.POINTER(ExtrapStats)]
         L.astg_mean_temperature_noalloc.argtypes = [c_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int, c_p, c_p,
@@ -261,6 +264,19 @@ class OctreeSmoke3:
         self._check(lib().astg_extrapolate(self._h, field.encode(), g.ctypes.data, res, valid_offset,
                                            max_distance_factor, ctypes.byref(st)))
         return st
+
+    def restart(self, directory, frame=0, layout=True):
+        """OctreeOmniGridSolver3::restart from <directory>/layout.bin, tilt.bin, density.bin, heat.bin
+        and velocity.bin (the reference's binary dumps)."""
+        f = lambda n: os.path.join(directory, n).encode()
+        self._check(lib().astg_restart(self._h, frame, f("layout.bin") if layout else None, f("boundary.bin"),
+                                       f("tilt.bin"), f("density.bin"), f("heat.bin"), f("velocity.bin")))
+
+    def save_checkpoint(self, directory):
+        """The reference's binary dumps of the current state into <directory>."""
+        f = lambda n: os.path.join(directory, n).encode()
+        self._check(lib().astg_save_checkpoint(self._h, f("layout.bin"), f("tilt.bin"), f("density.bin"),
+                                               f("heat.bin"), f("velocity.bin")))
 
     def max_velocity(self):
         v = ctypes.c_double()

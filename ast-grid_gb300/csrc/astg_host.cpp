@@ -9,6 +9,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <iterator>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -17,6 +19,8 @@
 #include "astg.h"
 #include "astg_launch.h"
 #include "scene.h"
+
+#include <sys/stat.h>
 
 using namespace astg;
 
@@ -778,6 +782,268 @@ struct astg_handle {
         }
     }
 
+    // ---------------------------------------------------------------- checkpoints
+    // The binary dumps of src/viewer/grid_dump.cpp:280-615 (native little-endian, LP64): a level
+    // count, then per level an entry count and the entries.  LayerNode3 (include/octree_layer3.h:
+    // 11-20) and TiltENode (include/tilt_e_node.h:15-31) are written as their 24-byte structs; the
+    // padding bytes carry no data (the reference leaves them uninitialised, they are written as 0).
+    struct Reader {
+        std::string file;
+        std::vector<char> buf;
+        size_t at = 0;
+        explicit Reader(const std::string& f) : file(f) {
+            std::ifstream in(f, std::ios::binary);
+            if (!in) throw std::invalid_argument("checkpoint: cannot open " + f);
+            buf.assign(std::istreambuf_iterator<char>(in), std::istreambuf_iterator<char>());
+        }
+        void raw(void* dst, size_t n) {
+            if (at + n > buf.size()) throw std::invalid_argument("checkpoint " + file + ": truncated");
+            memcpy(dst, buf.data() + at, n);
+            at += n;
+        }
+        int i32() { int32_t v; raw(&v, 4); return v; }
+        long long i64() { int64_t v; raw(&v, 8); return v; }
+        double f64() { double v; raw(&v, 8); return v; }
+        void end() {
+            if (at != buf.size()) throw std::invalid_argument("checkpoint " + file + ": trailing bytes");
+        }
+    };
+    struct Writer {
+        std::string file;
+        std::vector<char> buf;
+        void raw(const void* src, size_t n) { buf.insert(buf.end(), (const char*)src, (const char*)src + n); }
+        void i32(int v) { int32_t x = v; raw(&x, 4); }
+        void i64(long long v) { int64_t x = v; raw(&x, 8); }
+        void f64(double v) { raw(&v, 8); }
+        void save() {
+            // create the parent directories, as the reference's createDir does (src/util.cpp:50-58)
+            for (size_t p = file.find('/', 1); p != std::string::npos; p = file.find('/', p + 1))
+                mkdir(file.substr(0, p).c_str(), 0755);
+            std::ofstream out(file, std::ios::binary);
+            if (!out) throw std::invalid_argument("checkpoint: cannot write " + file);
+            out.write(buf.data(), buf.size());
+            if (!out) throw std::runtime_error("checkpoint: write failed: " + file);
+        }
+    };
+    long long coor3(int s) const {  // PACK_COOR3 (include/macro.h:39): a layer's own keys, no level
+        return ((long long)sx[s] << 40) | ((long long)sy[s] << 20) | (long long)sz[s];
+    }
+    long long lcoor(int s) const {  // PACK_LCOOR3, include/macro.h:39-45
+        return ((long long)slev[s] << 60) | ((long long)sx[s] << 40) | ((long long)sy[s] << 20) | (long long)sz[s];
+    }
+    uint32_t nodeFlag(int s) const {  // VALID | IS_GHOST | GHOST_FROM_COARSE
+        return 1u | ((sflag[s] & SF_GHOST) ? 2u : 0u) | ((sflag[s] & SF_FROM_COARSE) ? 4u : 0u);
+    }
+    void writeLayout(const std::string& f) {
+        Writer w{f, {}};
+        w.i32(L);
+        for (int l = 0; l < L; ++l) {
+            int n = lN[l], g = lG[l];
+            w.i32(n + g);
+            for (int i = 0; i < n + g; ++i) {
+                int s = loff[l] + i;
+                unsigned char node[24] = {0};
+                uint64_t index = (uint64_t)i;
+                uint16_t xyz[3] = {(uint16_t)sx[s], (uint16_t)sy[s], (uint16_t)sz[s]};
+                uint32_t flag = nodeFlag(s);
+                memcpy(node, &index, 8);
+                memcpy(node + 8, xyz, 6);
+                memcpy(node + 16, &flag, 4);
+                w.i64(coor3(s));
+                w.raw(node, 24);
+            }
+            w.i32(g);
+            for (int i = n; i < n + g; ++i) w.i64(coor3(loff[l] + i));
+            w.i32(n);
+            for (int i = 0; i < n; ++i) w.i64(coor3(loff[l] + i));
+        }
+        w.i32((int)half.size());
+        for (int hs : half) w.i64(lcoor(hs));
+        w.save();
+    }
+    // readOctreeLayout3dBinary into an existing layout keeps the handle's octree: the file must
+    // describe the same nodes (the library does not rebuild its octree on restart)
+    void checkLayout(const std::string& f) {
+        Reader r(f);
+        auto fail = [&](const std::string& what) {
+            throw std::runtime_error("checkpoint " + f + ": layout differs from the handle's (" + what + ")");
+        };
+        if (r.i32() != L) fail("level count");
+        for (int l = 0; l < L; ++l) {
+            int n = lN[l], g = lG[l];
+            int m = r.i32();
+            if (m != n + g) fail("nodes of level " + std::to_string(l));
+            for (int k = 0; k < m; ++k) {
+                long long c = r.i64();
+                unsigned char node[24];
+                r.raw(node, 24);
+                uint64_t index;
+                uint16_t xyz[3];
+                uint32_t flag;
+                memcpy(&index, node, 8);
+                memcpy(xyz, node + 8, 6);
+                memcpy(&flag, node + 16, 4);
+                if (index >= (uint64_t)m) fail("node index");
+                int s = loff[l] + (int)index;
+                if (c != coor3(s) || xyz[0] != sx[s] || xyz[1] != sy[s] || xyz[2] != sz[s] || (flag & 7u) != nodeFlag(s))
+                    fail("node of level " + std::to_string(l));
+            }
+            if (r.i32() != g) fail("ghosts of level " + std::to_string(l));
+            for (int i = n; i < n + g; ++i)
+                if (r.i64() != coor3(loff[l] + i)) fail("ghost order of level " + std::to_string(l));
+            if (r.i32() != n) fail("cells of level " + std::to_string(l));
+            for (int i = 0; i < n; ++i)
+                if (r.i64() != coor3(loff[l] + i)) fail("cell order of level " + std::to_string(l));
+        }
+        if (r.i32() != (int)half.size()) fail("half tilts");
+        for (int hs : half)
+            if (r.i64() != lcoor(hs)) fail("half tilt order");
+        r.end();
+    }
+    // per-level record arrays of `width` doubles per slot
+    void writeLevels(Writer& w, const std::vector<double>& v, int width) {
+        w.i32(L);
+        for (int l = 0; l < L; ++l) {
+            int m = lN[l] + lG[l];
+            w.i32(m);
+            w.raw(v.data() + (size_t)loff[l] * width, (size_t)m * width * 8);
+        }
+    }
+    void readLevels(Reader& r, std::vector<double>& v, int width) {
+        if (r.i32() != L) throw std::invalid_argument("checkpoint " + r.file + ": level count differs");
+        v.assign((size_t)S * width, 0.0);
+        for (int l = 0; l < L; ++l) {
+            int m = lN[l] + lG[l];
+            if (r.i32() != m) throw std::invalid_argument("checkpoint " + r.file + ": level size differs");
+            r.raw(v.data() + (size_t)loff[l] * width, (size_t)m * width * 8);
+        }
+    }
+    void saveCheckpoint(const char* layoutF, const char* tiltF, const char* densityF, const char* heatF,
+                        const char* velocityF) {
+        if (layoutF) writeLayout(layoutF);
+        if (tiltF) {
+            std::vector<double> e(S);
+            std::vector<int32_t> fl(2 * (size_t)S);
+            getArray("tilt_e", e.data(), 8 * (size_t)S);
+            getArray("tilt_flags", fl.data(), 8 * (size_t)S);
+            Writer w{tiltF, {}};
+            w.i32(L);
+            for (int l = 0; l < L; ++l) {
+                int m = lN[l] + lG[l];
+                w.i32(m);
+                for (int i = 0; i < m; ++i) {
+                    int s = loff[l] + i;
+                    unsigned char node[24] = {0};
+                    memcpy(node, &e[s], 8);
+                    for (int b = 0; b < 6; ++b) node[8 + b] = (fl[2 * s] >> b) & 1;
+                    int32_t dir = fl[2 * s + 1];
+                    memcpy(node + 16, &dir, 4);
+                    w.raw(node, 24);
+                }
+            }
+            w.save();
+        }
+        auto scalar = [&](const char* f, const char* oct, const char* til) {
+            std::vector<double> o(S), t(S);
+            getArray(oct, o.data(), 8 * (size_t)S);
+            getArray(til, t.data(), 8 * (size_t)S);
+            Writer w{f, {}};
+            writeLevels(w, o, 1);
+            writeLevels(w, t, 1);
+            w.save();
+        };
+        if (densityF) scalar(densityF, "density_oct", "density_tilt");
+        if (heatF) scalar(heatF, "heat_oct", "heat_tilt");
+        if (velocityF) {
+            std::vector<double> mac(3 * (size_t)S), tv(8 * (size_t)S);
+            getArray("mac", mac.data(), 24 * (size_t)S);
+            getArray("tilt_vel", tv.data(), 64 * (size_t)S);
+            Writer w{velocityF, {}};
+            for (int a = 0; a < 3; ++a) {
+                std::vector<double> u(mac.begin() + (size_t)a * S, mac.begin() + (size_t)(a + 1) * S);
+                writeLevels(w, u, 1);
+            }
+            writeLevels(w, tv, 8);
+            w.save();
+        }
+    }
+    // OctreeOmniGridSolver3::restart (src/octree_omnigrid_solver3.cpp:1015-1057): tilt-E, density,
+    // heat and velocity into both buffers, then the velocity ghosts, the dual grid and its ghosts
+    // of both.  The boundary file is not read (the reference does not read it either); the
+    // tilt open/closed layout flags stay as they are, as in the reference.
+    void restart(const char* layoutF, const char* tiltF, const char* densityF, const char* heatF,
+                 const char* velocityF) {
+        if (!tiltF || !densityF || !heatF || !velocityF)
+            throw std::invalid_argument("astg_restart: tilt, density, heat and velocity files are required");
+        if (layoutF) checkLayout(layoutF);
+        // read everything before touching the handle, so a bad file leaves the state as it was
+        std::vector<double> e(S), dO, dT, hO, hT, ux, uy, uz, tv;
+        std::vector<int32_t> fl(2 * (size_t)S);
+        {
+            Reader r(tiltF);
+            if (r.i32() != L) throw std::invalid_argument("checkpoint " + r.file + ": level count differs");
+            for (int l = 0; l < L; ++l) {
+                int m = lN[l] + lG[l];
+                if (r.i32() != m) throw std::invalid_argument("checkpoint " + r.file + ": level size differs");
+                for (int i = 0; i < m; ++i) {
+                    int s = loff[l] + i;
+                    unsigned char node[24];
+                    r.raw(node, 24);
+                    memcpy(&e[s], node, 8);
+                    int f = 0;
+                    for (int b = 0; b < 6; ++b) f |= (node[8 + b] ? 1 : 0) << b;
+                    int32_t dir;
+                    memcpy(&dir, node + 16, 4);
+                    fl[2 * s] = f;
+                    fl[2 * s + 1] = dir;
+                }
+            }
+            r.end();
+        }
+        {
+            Reader r(densityF);
+            readLevels(r, dO, 1);
+            readLevels(r, dT, 1);
+            r.end();
+        }
+        {
+            Reader r(heatF);
+            readLevels(r, hO, 1);
+            readLevels(r, hT, 1);
+            r.end();
+        }
+        {
+            Reader r(velocityF);
+            readLevels(r, ux, 1);
+            readLevels(r, uy, 1);
+            readLevels(r, uz, 1);
+            readLevels(r, tv, 8);
+            r.end();
+        }
+        std::vector<double> mac;
+        mac.reserve(3 * (size_t)S);
+        mac.insert(mac.end(), ux.begin(), ux.end());
+        mac.insert(mac.end(), uy.begin(), uy.end());
+        mac.insert(mac.end(), uz.begin(), uz.end());
+        for (const char* p : {"", "t_"}) {
+            std::string q = p;
+            setArray(q + "tilt_e", e.data(), 8 * (size_t)S);
+            setArray(q + "tilt_flags", fl.data(), 8 * (size_t)S);
+            setArray(q + "density_oct", dO.data(), 8 * (size_t)S);
+            setArray(q + "density_tilt", dT.data(), 8 * (size_t)S);
+            setArray(q + "heat_oct", hO.data(), 8 * (size_t)S);
+            setArray(q + "heat_tilt", hT.data(), 8 * (size_t)S);
+            setArray(q + "mac", mac.data(), 24 * (size_t)S);
+            setArray(q + "tilt_vel", tv.data(), 64 * (size_t)S);
+        }
+        for (int b : {cur, 1 - cur}) {
+            launch_velocity_ghost(d, F[b], dLastWriter, st);
+            launch_dual(d, F[b], st);
+        }
+        ck(cudaStreamSynchronize(st), "restart");
+        checkStatus();
+    }
+
     void readSolveStats() {
         int isc[ISC_COUNT], n = 0, nnz = 0;
         double sc[SC_COUNT];
@@ -1230,6 +1496,21 @@ astg_status astg_max_velocity(astg_handle* h, double* out) {
         for (double v : mac) m = std::max(m, v);
         *out = m;
     });
+}
+
+astg_status astg_restart(astg_handle* h, int frame, const char* layout_file, const char* boundary_file,
+                         const char* tilt_file, const char* density_file, const char* heat_file,
+                         const char* velocity_file) {
+    (void)frame;
+    (void)boundary_file;
+    if (!h) return ASTG_BAD_ARG;
+    return guard(h, [&] { h->restart(layout_file, tilt_file, density_file, heat_file, velocity_file); });
+}
+
+astg_status astg_save_checkpoint(astg_handle* h, const char* layout_file, const char* tilt_file,
+                                 const char* density_file, const char* heat_file, const char* velocity_file) {
+    if (!h) return ASTG_BAD_ARG;
+    return guard(h, [&] { h->saveCheckpoint(layout_file, tilt_file, density_file, heat_file, velocity_file); });
 }
 
 astg_status astg_extrapolate(astg_handle* h, const char* field, const double* sdf, int sdf_res, double valid_offset,

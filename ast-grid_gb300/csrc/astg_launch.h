@@ -149,6 +149,7 @@ struct LevelSpans {
 cudaError_t launch_mean_temperature_static(const double* heat, const LevelSpans& sp, double* amb, cudaStream_t st);
 void launch_force(const Dev& d, const Fields& F, const uint8_t* open, const double* amb, double dt, cudaStream_t st);
 void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);
+void launch_velocity_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);
 void launch_dof_numbering(const Dev& d, const uint8_t* open, Proj& P, cudaStream_t st);
 void launch_assemble(const Dev& d, const Fields& F, const uint8_t* open, Proj& P, const int* hoPtr, const int* hoIdx,
                      double dt, cudaStream_t st);

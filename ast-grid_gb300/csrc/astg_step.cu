@@ -299,6 +299,10 @@ __global__ void k_tilt_ghost(Dev d, Fields F, int l) {
 }
 void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st) {
     ASTG_LAUNCH(k_walls<<<nblk(d.S), TB, 0, st>>>(d, F.mac));
+    launch_velocity_ghost(d, F, lastWriter, st);
+}
+// OctreeOmniFaceCenteredGrid3::updateGhost (include/octree_omni_face_centered_grid3.h:97-120)
+void launch_velocity_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st) {
     ASTG_LAUNCH(k_mac_ghost_zero<<<nblk(d.S), TB, 0, st>>>(d, F.mac));
     for (int l = 0; l < d.L; ++l)
         if (d.lG[l]) ASTG_LAUNCH(k_mac_ghost_sample<<<nblk(d.lG[l]), TB, 0, st>>>(d, F.mac, l, 0));

@@ -144,6 +144,24 @@ astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32
  * (src/octree_omnigrid_solver3.cpp:1066-1122). */
 astg_status astg_max_velocity(astg_handle* h, double* out);
 
+/* OctreeOmniGridSolver3::restart (src/octree_omnigrid_solver3.cpp:1015-1057) from the reference's
+ * binary dumps (src/viewer/grid_dump.cpp:280-615, the files saveResult writes with saveStatus):
+ * tilt-E, density, heat and velocity go into both buffers, then the velocity ghosts, the dual grid
+ * and its ghosts are recomputed.  layout_file (may be NULL) must describe the handle's own octree
+ * (same nodes, order and flags), else ASTG_LAYOUT_ERROR; the octree is not rebuilt.  boundary_file
+ * is not read and frame is not kept, as in the reference.  A file that cannot be read, is
+ * truncated or has other sizes returns ASTG_BAD_ARG and leaves the state unchanged. */
+astg_status astg_restart(astg_handle* h, int frame, const char* layout_file, const char* boundary_file,
+                         const char* tilt_file, const char* density_file, const char* heat_file,
+                         const char* velocity_file);
+
+/* The dumps saveResult writes with saveStatus (src/octree_omnigrid_solver3.cpp:148, 996-1007;
+ * dumpOctreeLayout3dBinary, dumpOctreeOmniTiltE3dBinary, dumpOctreeOmniScalar3dBinary,
+ * dumpOctreeOmniFaceCentered3dBinary in src/viewer/grid_dump.cpp) of the current state, readable
+ * by the reference's restart; NULL skips a file; parent directories are created. */
+astg_status astg_save_checkpoint(astg_handle* h, const char* layout_file, const char* tilt_file,
+                                 const char* density_file, const char* heat_file, const char* velocity_file);
+
 typedef struct astg_extrap_stats {
     long long assigned;   /* nodes given an extrapolated value */
     int passes;           /* parallel passes (dependency rounds) used */

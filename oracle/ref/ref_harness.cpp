@@ -22,6 +22,7 @@
 #include "octree_util.h"
 #include "advection.h"
 #include "jet/fmm_levelset_solver3.h"
+#include "viewer/grid_dump.h"
 #include "scene.h"
 
 #include <cstdio>
@@ -89,6 +90,10 @@ struct Options {
     bool stages = false;
     // FmmLevelSetSolver3::extrapolate of the density after the steps: sphere SDF (centre, radius),
     // maximum distance factor, validity offset (known where sdf < -offset * d)
+    // checkpoint: after step ckptAt, write the reference's own binary dumps into ckptDir; restart:
+    // start from such dumps through OctreeOmniGridSolver3::restart instead of the initial noise
+    int ckptAt = -1;
+    std::string ckptDir, restartDir;
     bool extrap = false;
     double exC[3] = {0, 0, 0}, exR = 0, exMax = 0, exOff = 0;
     std::string out = "ref_out";
@@ -228,6 +233,15 @@ public:
     }
 
     void setTolerance() { pcgSolver.set_solver_parameters(opt.tol, 3000); }
+    // the reference's own dump functions (src/viewer/grid_dump.cpp:280-615) on the current state,
+    // the files saveResult writes with saveStatus (src/octree_omnigrid_solver3.cpp:148, 996-1007)
+    void writeCheckpoint(const std::string& d) {
+        dumpOctreeLayout3dBinary(d + "/layout.bin", *layout);
+        dumpOctreeOmniTiltE3dBinary(d + "/tilt.bin", *tiltE);
+        dumpOctreeOmniScalar3dBinary(d + "/density.bin", *density);
+        dumpOctreeOmniScalar3dBinary(d + "/heat.bin", *heat);
+        dumpOctreeOmniFaceCentered3dBinary(d + "/velocity.bin", *velocity);
+    }
     int pcgItersN() const { return (int)b.size(); }
 
     // ------------------------------------------------------------ dumps
@@ -460,6 +474,9 @@ int main(int argc, char** argv) {
         else if (a == "--stages") o.stages = true;
         else if (a == "--out") o.out = next();
         else if (a == "--source") parseSource(next(), o.src);
+        else if (a == "--checkpoint-at") o.ckptAt = atoi(next());
+        else if (a == "--checkpoint-dir") o.ckptDir = next();
+        else if (a == "--restart") o.restartDir = next();
         else if (a == "--extrapolate") {
             o.extrap = true;
             if (sscanf(next(), "%lf,%lf,%lf,%lf,%lf,%lf", &o.exC[0], &o.exC[1], &o.exC[2], &o.exR, &o.exMax, &o.exOff) != 6)
@@ -473,7 +490,17 @@ int main(int argc, char** argv) {
     Harness h(o, res);
     h.initialize();
     h.setTolerance();
-    h.initNoise();
+    if (o.restartDir.empty()) {
+        h.initNoise();
+    } else {
+        const std::string& d = o.restartDir;
+        if (!h.restart(0, d + "/layout.bin", d + "/boundary.bin", d + "/tilt.bin", d + "/density.bin", d + "/heat.bin",
+                       d + "/velocity.bin"))
+            throw std::runtime_error("restart failed");
+        Archive ra;
+        h.dumpState(ra, "restart/");
+        ra.write(o.out + "/restart.astg");
+    }
 
     Archive lay;
     h.dumpLayout(lay);
@@ -500,6 +527,7 @@ int main(int argc, char** argv) {
             h.stageAr.write(o.out + name);
         }
         fprintf(stderr, "step %d: n=%d iters=%d err=%.3e %.3fs\n", s + 1, (int)h.pcgItersN(), h.pcgIters, h.pcgErr, secs);
+        if (s + 1 == o.ckptAt) h.writeCheckpoint(o.ckptDir);
     }
     for (int l = 0; l < h.levels(); ++l)
         if (h.getLayout()->levelSize(l) != sizes0[l]) fprintf(stderr, "warning: level %d grew during the run\n", l);

@@ -19,6 +19,14 @@ FmmLevelSetSolver3::extrapolate (after/density_oct, after/density_tilt), meta/ca
 meta/extrap = [cx, cy, cz, r, max_distance_factor, offset].
 
     python tests/golden/make_golden.py --extrap-only
+
+Checkpoint fixtures (ref_ckpt_*.npz): the reference's own dump files after `steps` steps
+(file/layout.bin, file/tilt.bin, file/density.bin, file/heat.bin, file/velocity.bin, as raw bytes),
+the state it restores from them with OctreeOmniGridSolver3::restart in a fresh solver
+(restart/<field>, restart/t_<field>) and its first step after that restart (step1/<field> and the
+projection, as in the step fixtures).
+
+    python tests/golden/make_golden.py --ckpt-only
 """
 import os
 import subprocess
@@ -38,6 +46,10 @@ CASES = [
     ("ref_c16_l2", 16, 2, 3, False),
 ]
 STAGES = ["scene", "force", "preproject", "project", "dual", "advect"]
+CKPT_CASES = [
+    # name, coarsest, levels, steps before the checkpoint
+    ("ref_ckpt_c8_l3", 8, 3, 2),
+]
 EXTRAP_CASES = [
     # name, coarsest, levels, steps, (centre x, y, z, radius, max distance factor, validity offset)
     ("ref_extrap_c8_l3", 8, 3, 2, (0.47, 0.53, 0.29, 0.15, 4.0, 0.0)),
@@ -67,13 +79,41 @@ def extrap_fixtures(harness):
             print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB, {len(out)} arrays")
 
 
+def ckpt_fixtures(harness):
+    for name, c, lv, steps in CKPT_CASES:
+        with tempfile.TemporaryDirectory() as d:
+            files, a, b = (os.path.join(d, x) for x in ("files", "a", "b"))
+            os.makedirs(a)
+            os.makedirs(b)
+            base = [harness, "--coarsest", str(c), "--levels", str(lv)]
+            subprocess.check_call(base + ["--steps", str(steps), "--out", a, "--checkpoint-at", str(steps),
+                                          "--checkpoint-dir", files], cwd=d)
+            subprocess.check_call(base + ["--steps", "1", "--out", b, "--restart", files], cwd=d)
+            out = {}
+            for f in ("layout.bin", "tilt.bin", "density.bin", "heat.bin", "velocity.bin"):
+                out["file/" + f] = np.fromfile(os.path.join(files, f), dtype=np.uint8)
+            out.update(astg_archive.read(os.path.join(b, "restart.astg")))
+            st = astg_archive.read(os.path.join(b, "step_0001.astg"))
+            for key, v in st.items():
+                if key != "wall_s":
+                    out[f"step1/{key}"] = v
+            out["meta/case"] = np.array([c, lv, steps], dtype=np.int32)
+            path = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(path, **out)
+            print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB, {len(out)} arrays")
+
+
 def main():
     ref = os.environ.get("ASTG_REF", "/root/reference")
     subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref", "Makefile"), f"REF={ref}",
                            "-j8"])
     harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
-    extrap_fixtures(harness)
+    if "--ckpt-only" not in sys.argv:
+        extrap_fixtures(harness)
     if "--extrap-only" in sys.argv:
+        return
+    ckpt_fixtures(harness)
+    if "--ckpt-only" in sys.argv:
         return
     for name, c, lv, steps, stages in CASES:
         with tempfile.TemporaryDirectory() as d:
