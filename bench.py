@@ -333,7 +333,12 @@ def run_ours(args):
              "dtype": "f32 inner / f64 outer", "stopping_test": "|b - A x|_inf <= 1e-6 |b|_inf in FP64"}
     s.set_precision("fp64")
 
-    # ---------------- end to end through the C ABI with pinned host buffers
+    # ---------------- end to end through the C ABI with pinned host buffers, on a second handle
+    # with the same warm-up, so that it covers the same steps of the simulation as `value`
+    s.close()
+    s = ast_solver.OctreeSmoke3(COARSEST, LEVELS, device=local)
+    for _ in range(args.warmup):
+        s.update(DT)
     names_sync = ["density_oct", "density_tilt", "heat_oct", "heat_tilt"]
     host = {n: torch.empty(S, dtype=torch.float64, pin_memory=True) for n in names_sync}
     out = torch.empty(S, dtype=torch.float64, pin_memory=True)
@@ -425,7 +430,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=10, help="steps of the end-to-end loop")
+    ap.add_argument("--e2e-steps", type=int, default=20, help="steps of the end-to-end loop (at most --steps)")
     ap.add_argument("--solve-steps", type=int, default=100, help="steps before the isolated solves")
     ap.add_argument("--solve-rhs", type=int, default=20, help="right-hand sides of the isolated solves (0: skip)")
     args = ap.parse_args()
