@@ -20,10 +20,21 @@ struct KProf {
     bool on = false;
     double ms[KPROF_KINDS] = {0, 0, 0, 0};
     long long count[KPROF_KINDS] = {0, 0, 0, 0};
-    cudaEvent_t ev[2 * 128];
+    cudaEvent_t ev[2 * 128];  // pairs recorded by direct launches since the last drain
     int kind[128];
     int used = 0;
+    cudaEvent_t gev[2 * 64];  // pairs recorded by the nodes of the current PCG batch graph
+    int gkind[64];
+    int gused = 0;
     bool created = false;
+    KProf() = default;
+    KProf(const KProf&) = delete;
+    KProf& operator=(const KProf&) = delete;
+    ~KProf() {
+        if (!created) return;
+        for (auto& e : ev) cudaEventDestroy(e);
+        for (auto& e : gev) cudaEventDestroy(e);
+    }
 };
 
 constexpr int ROW_W = 32;   // padded row width during assembly (rows have at most ~21 entries)

@@ -28,33 +28,116 @@ namespace astg {
 
 long long g_launches = 0;
 
-// event pairs around profiled launches; drained after each host synchronisation
+// event pairs around profiled launches; drained after each host synchronisation.  On a capturing
+// stream the records become event-record nodes of the graph (external records) in a separate set
+// of pairs, which every replay records again.
+static bool capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive;
+}
 static void prof_begin(KProf* p, int kind, cudaStream_t st) {
     if (!p || !p->on) return;
     if (!p->created) {
         for (auto& e : p->ev) cudaEventCreate(&e);
+        for (auto& e : p->gev) cudaEventCreate(&e);
         p->created = true;
     }
-    if (p->used >= 128) return;
-    p->kind[p->used] = kind;
-    cudaEventRecord(p->ev[2 * p->used], st);
+    if (capturing(st)) {
+        if (p->gused >= 64) return;
+        p->gkind[p->gused] = kind;
+        cudaEventRecordWithFlags(p->gev[2 * p->gused], st, cudaEventRecordExternal);
+    } else {
+        if (p->used >= 128) return;
+        p->kind[p->used] = kind;
+        cudaEventRecord(p->ev[2 * p->used], st);
+    }
 }
 static void prof_end(KProf* p, cudaStream_t st) {
-    if (!p || !p->on || p->used >= 128) return;
-    cudaEventRecord(p->ev[2 * p->used + 1], st);
-    ++p->used;
-}
-static void prof_drain(KProf* p) {
     if (!p || !p->on) return;
-    for (int i = 0; i < p->used; ++i) {
-        float ms = 0;
-        if (cudaEventElapsedTime(&ms, p->ev[2 * i], p->ev[2 * i + 1]) == cudaSuccess) {
-            p->ms[p->kind[i]] += ms;
-            p->count[p->kind[i]] += 1;
-        }
+    if (capturing(st)) {
+        if (p->gused >= 64) return;
+        cudaEventRecordWithFlags(p->gev[2 * p->gused + 1], st, cudaEventRecordExternal);
+        ++p->gused;
+    } else {
+        if (p->used >= 128) return;
+        cudaEventRecord(p->ev[2 * p->used + 1], st);
+        ++p->used;
     }
-    p->used = 0;
 }
+static void prof_add(KProf* p, cudaEvent_t a, cudaEvent_t b, int kind) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) {
+        p->ms[kind] += ms;
+        p->count[kind] += 1;
+    } else {
+        cudaGetLastError();  // a pair that was not recorded is not a launch error of the step
+    }
+}
+// direct pairs, and the graph's pairs when a replay ran since the last drain
+static void prof_drain(KProf* p, bool replayed = false) {
+    if (!p || !p->on) return;
+    for (int i = 0; i < p->used; ++i) prof_add(p, p->ev[2 * i], p->ev[2 * i + 1], p->kind[i]);
+    p->used = 0;
+    if (replayed)
+        for (int i = 0; i < p->gused; ++i) prof_add(p, p->gev[2 * i], p->gev[2 * i + 1], p->gkind[i]);
+}
+
+// One batch of PCG iterations, either launched directly or replayed from a CUDA graph captured
+// on the first full batch (the kernels skip themselves once the device's done flag is set, so a
+// batch is the same work every time).  Replaying saves the launch gaps of the ~9 small kernels of
+// an iteration.  Not used with the sync-free sweeps, whose epoch counter changes every launch.
+// While kernel profiling is on, one replay in KPROF_GRAPH_EVERY runs a second graph whose kernels
+// are bracketed by event-record nodes (those nodes cost about 3 us each), the others the plain one.
+bool g_pcg_graphs = getenv("ASTG_PCG_GRAPH") ? atoi(getenv("ASTG_PCG_GRAPH")) != 0 : true;
+constexpr int KPROF_GRAPH_EVERY = 4;
+struct BatchGraph {
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};  // plain, with profiling event nodes
+    long long launches[2] = {0, 0};                 // kernels per replay
+    bool failed = false;
+    long long replays = 0;
+    bool profiled = false;  // the last replay recorded the event pairs
+    ~BatchGraph() {
+        for (auto e : exec)
+            if (e) cudaGraphExecDestroy(e);
+    }
+    // runs body(nb, prof) for a full batch through a graph; returns false to run it directly
+    template <typename Body>
+    bool run(Body body, int nb, cudaStream_t st, KProf* prof) {
+        if (failed) return false;
+        const int k = (prof && prof->on && replays % KPROF_GRAPH_EVERY == 0) ? 1 : 0;
+        if (!exec[k]) {
+            if (k) prof->gused = 0;
+            long long l0 = g_launches;
+            if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                cudaGetLastError();
+                failed = true;
+                return false;
+            }
+            body(nb, k ? prof : nullptr);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&exec[k], g, 0);
+            if (g) cudaGraphDestroy(g);
+            launches[k] = g_launches - l0;
+            g_launches = l0;
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                exec[k] = nullptr;
+                failed = true;
+                return false;
+            }
+        }
+        if (cudaGraphLaunch(exec[k], st) != cudaSuccess) {
+            cudaGetLastError();
+            failed = true;
+            return false;
+        }
+        g_launches += launches[k];
+        ++replays;
+        profiled = k == 1;
+        return true;
+    }
+};
 
 constexpr int TB = 256;
 static inline int nblk(long long n) { return (int)((n + TB - 1) / TB); }
@@ -1663,25 +1746,31 @@ int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& e
     ASTG_LAUNCH(k_copy<<<nblk(maxRows), TB, 0, st>>>(z, s, P.nDof));
     int launched = 0;
     int hostDone = 0;
-    while (launched < maxIter) {
-        int nb = batch;
-        if (launched + nb > maxIter) nb = maxIter - launched;
+    auto body = [&](int nb, KProf* pf) {
         for (int it = 0; it < nb; ++it) {
-            prof_begin(prof, 2, st);
+            prof_begin(pf, 2, st);
             ASTG_LAUNCH(k_spmv_dot<<<chunks, RED_LANES, 0, st>>>(P, s, z, P.part));
-            prof_end(prof, st);
+            prof_end(pf, st);
             ASTG_LAUNCH(k_alpha<<<1, RED_LANES, 0, st>>>(P, P.part));
             ASTG_LAUNCH(k_update_xr<<<nblk(maxRows), TB, 0, st>>>(P, x, r, s, z));
             ASTG_LAUNCH(k_check<<<1, 1, 0, st>>>(P, maxIter));
-            precond(d, P, r, z, epoch, st, prof);
+            precond(d, P, r, z, epoch, st, pf);
             ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
             ASTG_LAUNCH(k_beta<<<1, RED_LANES, 0, st>>>(P, P.part));
             ASTG_LAUNCH(k_update_s<<<nblk(maxRows), TB, 0, st>>>(P, s, z));
         }
+    };
+    BatchGraph graph;
+    const bool graphs = g_pcg_graphs && (P.pcActive || P.clusterSize > 0);
+    while (launched < maxIter) {
+        int nb = batch;
+        if (launched + nb > maxIter) nb = maxIter - launched;
+        bool replayed = graphs && nb == batch && graph.run(body, nb, st, prof);
+        if (!replayed) body(nb, prof);
         launched += nb;
         cudaMemcpyAsync(P.hostDone, P.done, sizeof(int), cudaMemcpyDeviceToHost, st);
         cudaStreamSynchronize(st);
-        prof_drain(prof);
+        prof_drain(prof, replayed && graph.profiled);
         hostDone = *P.hostDone;
         if (hostDone) break;
     }
@@ -1841,6 +1930,7 @@ int launch_pcg_mixed(const Dev& d, Proj& P, double tolFactor, int maxIter, int b
     double res = res0;
     int outer = 0, converged = 0;
     PcaData<float> D = pca_data32(P);
+    BatchGraph graph;  // one inner batch; the same work in every outer cycle
     for (;;) {
         if (res <= tolAbs) {
             converged = 1;
@@ -1860,26 +1950,30 @@ int launch_pcg_mixed(const Dev& d, Proj& P, double tolFactor, int maxIter, int b
         ASTG_LAUNCH(k_tree_dot32<<<chunks, RED_LANES, 0, st>>>(P.z32, P.r32, P.nDof, P.part));
         ASTG_LAUNCH(k_inner_start<<<1, RED_LANES, 0, st>>>(P, P.part, innerTol));
         ASTG_LAUNCH(k_copy32<<<nblk(maxRows), TB, 0, st>>>(P.z32, P.s32, P.nDof));
-        for (int launched = 0; launched < maxIter;) {
-            for (int it = 0; it < batch; ++it) {
-                prof_begin(prof, 2, st);
+        auto body = [&](int nb, KProf* pf) {
+            for (int it = 0; it < nb; ++it) {
+                prof_begin(pf, 2, st);
                 ASTG_LAUNCH(k_spmv32_dot<<<chunks, RED_LANES, 0, st>>>(P, P.s32, P.q32, P.part));
-                prof_end(prof, st);
+                prof_end(pf, st);
                 ASTG_LAUNCH(k_alpha<<<1, RED_LANES, 0, st>>>(P, P.part));
                 ASTG_LAUNCH(k_update_er32<<<nblk(maxRows), TB, 0, st>>>(P));
                 ASTG_LAUNCH(k_check<<<1, 1, 0, st>>>(P, maxIter));
-                prof_begin(prof, 0, st);
-                e = launch_precond_async(d, P, D, P.z32, P.pcSmem32, st);
-                prof_end(prof, st);
-                if (e != cudaSuccess) g_cluster_error = e;
+                prof_begin(pf, 0, st);
+                cudaError_t pe = launch_precond_async(d, P, D, P.z32, P.pcSmem32, st);
+                prof_end(pf, st);
+                if (pe != cudaSuccess) g_cluster_error = pe;
                 ASTG_LAUNCH(k_tree_dot32<<<chunks, RED_LANES, 0, st>>>(P.z32, P.r32, P.nDof, P.part));
                 ASTG_LAUNCH(k_beta<<<1, RED_LANES, 0, st>>>(P, P.part));
                 ASTG_LAUNCH(k_update_s32<<<nblk(maxRows), TB, 0, st>>>(P));
             }
+        };
+        for (int launched = 0; launched < maxIter;) {
+            bool replayed = g_pcg_graphs && graph.run(body, batch, st, prof);
+            if (!replayed) body(batch, prof);
             launched += batch;
             cudaMemcpyAsync(P.hostDone, P.done, sizeof(int), cudaMemcpyDeviceToHost, st);
             cudaStreamSynchronize(st);
-            prof_drain(prof);
+            prof_drain(prof, replayed && graph.profiled);
             if (*P.hostDone) break;
         }
         ASTG_LAUNCH(k_add_correction<<<nblk(maxRows), TB, 0, st>>>(P, x));

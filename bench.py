@@ -376,7 +376,13 @@ def run_ours(args):
     fused_name = "k_precond_async" if form > 200 else "k_precond_dsmem"
     names = {"sweep_fwd": fused_name if fused else "k_sweep_fwd", "sweep_bwd": "k_sweep_bwd",
              "spmv_dot": "k_spmv_dot", "mic_factor": "k_mic_factor"}
-    top = max(kms, key=lambda k: kms[k][0])
+    # kernel times come from CUDA event pairs: every direct launch, and one PCG batch in four of
+    # the graph replays; rank kernels by their average launch time x launches per step
+    iters_per_step = float(np.mean(iters))
+    per_step = {"sweep_fwd": iters_per_step + 1, "sweep_bwd": iters_per_step + 1, "spmv_dot": iters_per_step,
+                "mic_factor": 1.0}
+    avg = {k: v[0] / v[1] for k, v in kms.items() if v[1] > 0}
+    top = max(avg, key=lambda k: avg[k] * per_step[k])
     n_mean = float(np.mean(dofs))
     nnz_mean = float(np.mean(nnzs))
     nnzL = (nnz_mean - n_mean) / 2  # strictly lower entries of the symmetric matrix
@@ -392,10 +398,11 @@ def run_ours(args):
         traffic = tr[f"{names[top]}_bytes_per_row"] * n_mean
     roofline = {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms, "launches": kms[top][1],
+                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms, "timed_launches": kms[top][1],
                 "note": "MIC(0) sweeps are bounded by the dependency chain (wavefront latency), not HBM",
                 "preconditioner_form": form}
-    kernel_breakdown = {names[k]: {"ms_total": v[0], "launches": v[1]} for k, v in kms.items()}
+    kernel_breakdown = {names[k]: {"avg_launch_ms": avg[k], "timed_launches": kms[k][1],
+                                   "est_ms_per_step": avg[k] * per_step[k]} for k in avg}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
