@@ -23,7 +23,8 @@ FP64, MIXED = 0, 1
 SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_stage",
            "astg_set_solver_parameters", "astg_set_precision", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
            "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate",
-           "astg_restart", "astg_save_checkpoint"]
+           "astg_restart", "astg_save_checkpoint", "astg_tape_start", "astg_tape_stop", "astg_adjoint_reset",
+           "astg_backward", "astg_step_vjp", "astg_stage_vjp", "astg_adjoint_probe", "astg_set_tilt_adaptivity"]
 
 
 class AstgError(RuntimeError):
@@ -34,6 +35,12 @@ class AstgError(RuntimeError):
 
 class ExtrapStats(ctypes.Structure):
     _fields_ = [("assigned", ctypes.c_longlong), ("passes", ctypes.c_int), ("ms", ctypes.c_double)]
+
+
+class AdjointStats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int), ("checkpoints", ctypes.c_int), ("recomputed_steps", ctypes.c_int),
+                ("solves", ctypes.c_int), ("pcg_iterations", ctypes.c_longlong), ("ms", ctypes.c_double),
+                ("ms_recompute", ctypes.c_double), ("tape_bytes", ctypes.c_longlong)]
 
 
 class Params(ctypes.Structure):
@@ -93,12 +100,21 @@ def lib(path=None):
                                        ctypes.POINTER(ExtrapStats)]
         L.astg_mean_temperature_noalloc.argtypes = [c_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int, c_p, c_p,
                                                     ctypes.c_char_p, ctypes.c_size_t]
+        L.astg_tape_start.argtypes = [c_p, ctypes.c_int]
+        L.astg_set_tilt_adaptivity.argtypes = [c_p, ctypes.c_int]
+        L.astg_tape_stop.argtypes = [c_p]
+        L.astg_adjoint_reset.argtypes = [c_p]
+        L.astg_backward.argtypes = [c_p, ctypes.POINTER(AdjointStats)]
+        L.astg_step_vjp.argtypes = [c_p, ctypes.c_double]
+        L.astg_stage_vjp.argtypes = [c_p, ctypes.c_int, ctypes.c_double]
+        L.astg_adjoint_probe.argtypes = [c_p, ctypes.c_int, ctypes.c_int, c_p, c_p]
         _lib = L
     return _lib
 
 
 _F64 = {"kernel_ms", "density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
-        "tilt_e", "w_mac", "w_tilt", "dual_tables", "A_val", "b", "p", "ambT"}
+        "tilt_e", "w_mac", "w_tilt", "dual_tables", "A_val", "b", "p", "ambT", "source_density_oct",
+        "source_density_tilt"}
 _I64 = {"half_tilts", "t_joints", "closed_by_half_tilt"}
 _U8 = {"tilt_open"}
 _SHAPES = {"mac": (3, -1), "tilt_vel": (-1, 8), "dual_oct": (-1, 3), "dual_tilt": (-1, 3), "tilt_flags": (-1, 2),
@@ -111,7 +127,10 @@ _FIELDS = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_
 
 
 def _base(name):
-    """Field name without the "t_" prefix that addresses the swap-partner buffer."""
+    """Field name without the "t_" prefix that addresses the swap-partner buffer, or the "adj_"
+    prefix of a cotangent array (same type and shape as the array it belongs to)."""
+    if name.startswith("adj_"):
+        return name[4:]
     return name[2:] if name.startswith("t_") and name[2:] in _FIELDS else name
 
 
@@ -212,7 +231,7 @@ class OctreeSmoke3:
     def slots(self):
         return self.size(0)
 
-    def get(self, name):
+    def _nbytes(self, name):
         need = ctypes.c_size_t(0)
         st = lib().astg_get(self._h, name.encode(), None, 0, ctypes.byref(need))
         if st != ASTG_BAD_ARG:  # a size query answers BAD_ARG with the size filled in
@@ -221,16 +240,80 @@ class OctreeSmoke3:
             err = lib().astg_last_error(self._h).decode()
             if "unknown" in err:
                 raise AstgError(st, err)
+        return need.value
+
+    def get(self, name):
+        nb = self._nbytes(name)
         dt = _dtype(name)
-        out = np.empty(need.value // np.dtype(dt).itemsize, dtype=dt)
+        out = np.empty(nb // np.dtype(dt).itemsize, dtype=dt)
         if out.size:
-            self._check(lib().astg_get(self._h, name.encode(), out.ctypes.data, need.value, None))
+            self._check(lib().astg_get(self._h, name.encode(), out.ctypes.data, nb, None))
         base = _base(name)
         return out.reshape(_SHAPES[base]) if base in _SHAPES else out
 
     def set(self, name, arr):
         a = np.ascontiguousarray(arr, dtype=_dtype(name)).ravel()
         self._check(lib().astg_set(self._h, name.encode(), a.ctypes.data, a.nbytes))
+
+    # torch tensors: the library copies straight from / into device (or host) memory
+    def get_tensor(self, name, device="cuda"):
+        import torch
+
+        if _dtype(name) is not np.float64:
+            raise ValueError("get_tensor: only f64 arrays")
+        nb = self._nbytes(name)
+        out = torch.empty(nb // 8, dtype=torch.float64, device=device)
+        if out.is_cuda:
+            torch.cuda.current_stream(out.device).synchronize()
+        if out.numel():
+            self._check(lib().astg_get(self._h, name.encode(), out.data_ptr(), nb, None))
+        base = _base(name)
+        return out.reshape(_SHAPES[base]) if base in _SHAPES else out
+
+    def set_tensor(self, name, t):
+        import torch
+
+        t = t.detach().to(torch.float64).contiguous()
+        if t.is_cuda:
+            torch.cuda.current_stream(t.device).synchronize()
+        self._check(lib().astg_set(self._h, name.encode(), t.data_ptr(), t.numel() * 8))
+
+    # ---- reverse mode (topology frozen: tilt adaptivity off)
+    def set_tilt_adaptivity(self, on):
+        """enableTiltAdaptivity; turning it off freezes the current tilt layout in both buffers."""
+        self._check(lib().astg_set_tilt_adaptivity(self._h, 1 if on else 0))
+
+    def tape_start(self, checkpoint_every=0):
+        """Records the following update() calls for backward(); checkpoint_every = k > 0 keeps the
+        state every k steps and recomputes the rest, 0 keeps every step's advection input."""
+        self._check(lib().astg_tape_start(self._h, checkpoint_every))
+
+    def tape_stop(self):
+        self._check(lib().astg_tape_stop(self._h))
+
+    def adjoint_reset(self):
+        self._check(lib().astg_adjoint_reset(self._h))
+
+    def backward(self):
+        """Reverse pass over the taped steps: the adj_* arrays go from the cotangent of the final
+        state to that of the state at tape_start (see astg_backward).  Returns AdjointStats."""
+        st = AdjointStats()
+        self._check(lib().astg_backward(self._h, ctypes.byref(st)))
+        return st
+
+    def step_vjp(self, dt):
+        self._check(lib().astg_step_vjp(self._h, dt))
+
+    def stage_vjp(self, stage, dt):
+        self._check(lib().astg_stage_vjp(self._h, stage, dt))
+
+    def adjoint_probe(self, what, pos):
+        """Sampler weights at positions (n x 3): what 0 -> (n, 5), what 1 -> (n, 15); see astg.h."""
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        per = 5 if what == 0 else 15
+        out = np.zeros((len(p), per))
+        self._check(lib().astg_adjoint_probe(self._h, what, len(p), p.ctypes.data, out.ctypes.data))
+        return out
 
     # reference-style getters (copies, reference storage order)
     def getDensity(self):
@@ -294,3 +377,52 @@ def mean_temperature_noalloc(d_heat_oct, level_slots, d_amb, stream=0):
                                              len(slots), d_amb, stream or None, err, len(err))
     if st != ASTG_OK:
         raise AstgError(st, err.value.decode())
+
+
+def _autograd_function():
+    import torch
+
+    class OctreeSmokeFunction(torch.autograd.Function):
+        """A differentiable window of octree smoke steps on one OctreeSmoke3 (created with
+        tilt_adaptivity=0, so the topology stays frozen over the window).
+
+        OctreeSmokeFunction.apply(solver, steps, dt, checkpoint_every, mac, tilt_vel,
+        source_density_oct, source_density_tilt) loads the velocity (MAC faces (3, S), tilted faces
+        (S, 8)) and the per-slot source densities into the solver, runs `steps` steps with the tape
+        on and returns the final octagon density (S,).  backward() runs the adjoint kernels
+        (astg_backward) and returns the gradients of those four inputs; the density and heat of
+        the starting state are the solver's own and receive none."""
+
+        @staticmethod
+        def forward(ctx, solver, steps, dt, checkpoint_every, mac, tilt_vel, src_oct, src_tilt):
+            solver.set_tensor("mac", mac)
+            solver.set_tensor("tilt_vel", tilt_vel)
+            solver.set_tensor("source_density_oct", src_oct)
+            solver.set_tensor("source_density_tilt", src_tilt)
+            solver.tape_start(checkpoint_every)
+            for _ in range(steps):
+                solver.update(dt)
+            ctx.solver = solver
+            ctx.device = mac.device
+            return solver.get_tensor("density_oct", mac.device)
+
+        @staticmethod
+        def backward(ctx, grad):
+            s = ctx.solver
+            s.adjoint_reset()
+            s.set_tensor("adj_density_oct", grad)
+            ctx.stats = s.backward()
+            dev = ctx.device
+            return (None, None, None, None, s.get_tensor("adj_mac", dev), s.get_tensor("adj_tilt_vel", dev),
+                    s.get_tensor("adj_source_density_oct", dev), s.get_tensor("adj_source_density_tilt", dev))
+
+    return OctreeSmokeFunction
+
+
+def __getattr__(name):
+    # torch is imported only when the autograd function is asked for
+    if name == "OctreeSmokeFunction":
+        fn = _autograd_function()
+        globals()[name] = fn
+        return fn
+    raise AttributeError(name)

@@ -114,6 +114,8 @@ struct Dev {
     double buoyD, buoyT, rho, decay;
     int closedMask;
     double srcX, srcY, srcZ, srcR;
+    const double* srcO;           // per slot: density the source sets on the octagon (default 1)
+    const double* srcT;           // per slot: density the source sets on the tilt / half tilt
 };
 
 struct Fields {

@@ -94,6 +94,8 @@ struct astg_handle {
     int* dHoPtr = nullptr;
     int* dHoIdx = nullptr;
     uint8_t* dLastWriter = nullptr;
+    double* dSrcO = nullptr;  // per-slot source densities (octagon, tilt)
+    double* dSrcT = nullptr;
     int* dStatus = nullptr;
     int epoch = 0;
     bool firstSource = true;
@@ -118,6 +120,7 @@ struct astg_handle {
 
     ~astg_handle() {
         if (st) cudaStreamSynchronize(st);
+        freeTape();
         for (void* p : allocs) cudaFree(p);
         if (J.hostDone) cudaFreeHost(J.hostDone);
         for (cudaEvent_t e : {ev0, ev1, evA, evB})
@@ -519,6 +522,10 @@ struct astg_handle {
         d.buoyD = P.buoy_density; d.buoyT = P.buoy_temp; d.rho = P.rho; d.decay = P.decay;
         d.closedMask = P.closed_mask;
         d.srcX = P.src_x; d.srcY = P.src_y; d.srcZ = P.src_z; d.srcR = P.src_r;
+        dSrcO = upload(std::vector<double>(S, 1.0));
+        dSrcT = upload(std::vector<double>(S, 1.0));
+        d.srcO = dSrcO;
+        d.srcT = dSrcT;
         dHoPtr = upload(hoPtr);
         dHoIdx = upload(hoIdx);
         dLastWriter = upload(lastWriter);
@@ -1135,7 +1142,13 @@ struct astg_handle {
 
     void step(double dt, astg_step_stats* out) {
         ck(cudaEventRecord(ev0, st), "event");
-        for (int i = 0; i < 6; ++i) stage(i, dt);
+        double* advDst = advTarget;
+        if (T.on && T.recording) advDst = tapeBeforeStep(dt);
+        for (int i = 0; i < 6; ++i) {
+            if (i == 5 && advDst) saveAdvectionInput(advDst);
+            stage(i, dt);
+        }
+        if (T.on && T.recording) ++T.steps;
         ck(cudaEventRecord(ev1, st), "event");
         checkStatus();
         if (out) {
@@ -1149,6 +1162,369 @@ struct astg_handle {
         }
     }
 
+    // ---------------------------------------------------------------- adjoint
+    // Reverse mode of astg_step with the topology frozen (tilt adaptivity off).  The cotangent of
+    // the state lives in GA[ga] (Fields layout; te / tf point at the frozen forward arrays), the
+    // source-density gradients in dGsO / dGsT.  Only the advection transpose reads field values of
+    // the forward state; the other stages are linear in the state with frozen coefficients.
+    Fields GA[2]{};
+    int ga = 0;
+    double* dGsO = nullptr;
+    double* dGsT = nullptr;
+    double* dGamb = nullptr;
+    double* dAdjB = nullptr;  // rows: cotangent of the pressure
+    int* dOwnJ = nullptr;
+    int* dOwnH = nullptr;
+    double ambInvCount = 0;
+    bool adjReady = false;
+    int adjN = -1;            // rows of the factorised system the adjoint solves use (-1: none)
+    long long adjSolves = 0, adjIters = 0;
+
+    void allocAdjoint() {
+        if (adjReady) return;
+        for (int b = 0; b < 2; ++b) {
+            GA[b].dO = dalloc<double>(S); GA[b].dT = dalloc<double>(S);
+            GA[b].hO = dalloc<double>(S); GA[b].hT = dalloc<double>(S);
+            GA[b].mac = dalloc<double>((size_t)3 * S);
+            GA[b].tv = dalloc<double>((size_t)8 * S);
+            GA[b].dualO = dalloc<double>((size_t)3 * S);
+            GA[b].dualT = dalloc<double>((size_t)3 * S);
+        }
+        dGsO = dalloc<double>(S);
+        dGsT = dalloc<double>(S);
+        dGamb = dalloc<double>(1);
+        dAdjB = dalloc<double>(J.rowsCap);
+        dOwnJ = dalloc<int>(S);
+        dOwnH = dalloc<int>(S);
+        long long count = 0;
+        for (int l = 0; l < L; ++l) count += (long long)(lN[l] + lG[l]) * (l == 0 ? 1 : 8);
+        ambInvCount = 1.0 / (double)count;
+        adjReady = true;
+        adjustFrozen();
+    }
+    // the frozen tilt-E arrays the transposes read, and the single writers of the ghost passes
+    void adjustFrozen() {
+        for (int b = 0; b < 2; ++b) { GA[b].te = F[cur].te; GA[b].tf = F[cur].tf; }
+        launch_adj_owners(d, F[cur].te, dOwnJ, dOwnH, st);
+    }
+    void zeroCotangent(Fields& g) {
+        ck(cudaMemsetAsync(g.dO, 0, 8 * (size_t)S, st), "memset");
+        ck(cudaMemsetAsync(g.dT, 0, 8 * (size_t)S, st), "memset");
+        ck(cudaMemsetAsync(g.hO, 0, 8 * (size_t)S, st), "memset");
+        ck(cudaMemsetAsync(g.hT, 0, 8 * (size_t)S, st), "memset");
+        ck(cudaMemsetAsync(g.mac, 0, 24 * (size_t)S, st), "memset");
+        ck(cudaMemsetAsync(g.tv, 0, 64 * (size_t)S, st), "memset");
+        ck(cudaMemsetAsync(g.dualO, 0, 24 * (size_t)S, st), "memset");
+        ck(cudaMemsetAsync(g.dualT, 0, 24 * (size_t)S, st), "memset");
+    }
+    void resetAdjoint() {
+        allocAdjoint();
+        zeroCotangent(GA[ga]);
+        ck(cudaMemsetAsync(dGsO, 0, 8 * (size_t)S, st), "memset");
+        ck(cudaMemsetAsync(dGsT, 0, 8 * (size_t)S, st), "memset");
+        ck(cudaStreamSynchronize(st), "sync");
+    }
+    // assembles and factorises the (state-independent) pressure matrix for the adjoint solves
+    void prepareAdjointSystem() {
+        launch_dof_numbering(d, dOpen, J, st);
+        int n = 0;
+        ck(cudaMemcpyAsync(&n, J.nDof, sizeof n, cudaMemcpyDeviceToHost, st), "dofs");
+        ck(cudaStreamSynchronize(st), "dofs");
+        if (n > J.rowsCap) throw std::runtime_error("projection has more rows than the workspace holds");
+        select_preconditioner(J, n);
+        launch_assemble(d, F[cur], dOpen, J, dHoPtr, dHoIdx, 1.0, st);
+        launch_factor(d, J, P.omega, P.min_diag, epoch, st, nullptr);
+        bool mixed = P.precision == ASTG_MIXED && J.pcActive32;
+        bool owner = mixed || (J.pcActive && J.pcAsync);
+        if (J.clusterSize > 0 || J.pcActive || mixed) launch_level_schedule(d, J, owner, st);
+        adjN = n;
+    }
+    // transpose of project(): u_bar -> p_bar (pressure update), lambda = A^-1 p_bar (A is
+    // symmetric), u_bar += B^T lambda (right-hand side of the assembly)
+    void projectAdjoint(double dt, const Fields& C, Fields& g) {
+        if (adjN < 0) prepareAdjointSystem();
+        ck(cudaMemsetAsync(dAdjB, 0, 8 * (size_t)J.rowsCap, st), "memset");
+        launch_adj_pressure_update(d, C, g, dOpen, J.pO, J.pT, dAdjB, dt, st);
+        ck(cudaMemcpyAsync(J.b, dAdjB, 8 * (size_t)adjN, cudaMemcpyDeviceToDevice, st), "copy");
+        bool mixed = P.precision == ASTG_MIXED && J.pcActive32;
+        if (mixed) launch_pcg_mixed(d, J, P.tol, P.max_iter, 8, st, nullptr);
+        else launch_pcg_fp64(d, J, P.tol, P.max_iter, epoch, 8, st, nullptr);
+        int it[2] = {0, 0};
+        ck(cudaMemcpyAsync(it, J.isc, sizeof it, cudaMemcpyDeviceToHost, st), "iters");
+        ck(cudaStreamSynchronize(st), "sync");
+        ++adjSolves;
+        adjIters += it[ISC_ITERS];
+        launch_adj_rhs(d, C, g, dOpen, J, dHoPtr, dHoIdx, J.x, P.rho / dt, st);
+    }
+    // cotangent of a stage's input from that of its output (GA[ga], in place); C is the stage's
+    // input state (field values are read by stage 5 only)
+    void adjStage(int id, double dt, const Fields& C, bool firstSrc) {
+        Fields& g = GA[ga];
+        switch (id) {
+            case 0:
+                if (firstSrc) {
+                    launch_adj_scalar_ghost(d, g.hO, g.hT, g.te, g.tf, dOwnJ, dOwnH, st);
+                    launch_adj_scalar_ghost(d, g.dO, g.dT, g.te, g.tf, dOwnJ, dOwnH, st);
+                }
+                if (P.src_r > 0) launch_adj_source(d, g, dGsO, dGsT, st);
+                break;
+            case 1: launch_adj_force(d, C, g, dOpen, dt, dGamb, ambInvCount, st); break;
+            case 2: launch_adj_walls_and_ghost(d, C, g, dLastWriter, st); break;
+            case 3: projectAdjoint(dt, C, g); break;
+            case 4:
+                launch_adj_dual(d, C, g, dOwnJ, dOwnH, st);
+                launch_adj_walls_and_ghost(d, C, g, dLastWriter, st);
+                break;
+            case 5: {
+                Fields& gc = GA[1 - ga];
+                zeroCotangent(gc);
+                launch_adj_advect(d, C, gc, g, dOpen, dt, dOwnJ, dOwnH, st);
+                ga = 1 - ga;
+                break;
+            }
+            default: throw std::invalid_argument("stage must be 0..5");
+        }
+        ck(cudaGetLastError(), "launch");
+    }
+    void requireFrozen(const char* what) {
+        if (P.tilt_adaptivity) throw std::invalid_argument(std::string(what) + ": needs tilt adaptivity off (frozen topology)");
+    }
+    // astg_stage_vjp: the current state is the stage's input
+    void stageVjp(int id, double dt) {
+        requireFrozen("astg_stage_vjp");
+        allocAdjoint();
+        adjustFrozen();
+        if (id == 3) prepareAdjointSystem();
+        adjStage(id, dt, F[cur], firstSource);
+        checkStatus();
+    }
+
+    // ---- tape: state needed to run the step transposes in reverse
+    // per step: the advection input (density, heat, MAC, dual), 13 S doubles; per checkpoint: both
+    // buffers of the state (dO dT hO hT mac tv dualO dualT), 42 S doubles
+    struct Tape {
+        bool on = false;
+        int recording = 1;
+        int every = 0;  // 0: keep each step's advection input, else a checkpoint every `every` steps
+        int steps = 0;
+        std::vector<double> dt;
+        std::vector<uint8_t> first;
+        std::vector<double*> adv;   // store mode: per step; checkpoint mode: per step of a segment
+        std::vector<double*> ckpt;
+        std::vector<int> ckCur;
+        std::vector<uint8_t> ckFirst;
+        double* endState = nullptr;
+        long long bytes = 0;
+    } T;
+    double* advTarget = nullptr;  // step() copies the advection input here when set
+    static constexpr size_t ADV_DOUBLES = 13;
+    static constexpr size_t FULL_DOUBLES = 42;
+    double* rawAlloc(size_t doubles) {
+        void* p = nullptr;
+        ck(cudaMalloc(&p, doubles * 8 * (size_t)S), "cudaMalloc (tape)");
+        return (double*)p;
+    }
+    double* tapeAlloc(size_t doubles) {
+        double* p = rawAlloc(doubles);
+        T.bytes += (long long)(doubles * 8 * (size_t)S);
+        return p;
+    }
+    void freeTape() {
+        if (st) cudaStreamSynchronize(st);
+        for (double* p : T.adv) cudaFree(p);
+        for (double* p : T.ckpt) cudaFree(p);
+        if (T.endState) cudaFree(T.endState);
+        T = Tape{};
+    }
+    void copyD(double* dst, const double* src, size_t n) {
+        ck(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyDeviceToDevice, st), "copy");
+    }
+    void saveAdvectionInput(double* o) {
+        const Fields& C = F[cur];
+        size_t n = S;
+        copyD(o, C.dO, n); copyD(o + n, C.dT, n); copyD(o + 2 * n, C.hO, n); copyD(o + 3 * n, C.hT, n);
+        copyD(o + 4 * n, C.mac, 3 * n); copyD(o + 7 * n, C.dualO, 3 * n); copyD(o + 10 * n, C.dualT, 3 * n);
+    }
+    Fields advectionView(double* o) const {
+        Fields C = F[cur];
+        size_t n = S;
+        C.dO = o; C.dT = o + n; C.hO = o + 2 * n; C.hT = o + 3 * n;
+        C.mac = o + 4 * n; C.dualO = o + 7 * n; C.dualT = o + 10 * n;
+        C.tv = nullptr;
+        return C;
+    }
+    void saveFull(double* o) {
+        size_t n = S;
+        for (int b = 0; b < 2; ++b) {
+            double* q = o + (size_t)b * 21 * n;
+            const Fields& G = F[b];
+            copyD(q, G.dO, n); copyD(q + n, G.dT, n); copyD(q + 2 * n, G.hO, n); copyD(q + 3 * n, G.hT, n);
+            copyD(q + 4 * n, G.mac, 3 * n); copyD(q + 7 * n, G.tv, 8 * n);
+            copyD(q + 15 * n, G.dualO, 3 * n); copyD(q + 18 * n, G.dualT, 3 * n);
+        }
+    }
+    void restoreFull(const double* o) {
+        size_t n = S;
+        for (int b = 0; b < 2; ++b) {
+            const double* q = o + (size_t)b * 21 * n;
+            Fields& G = F[b];
+            copyD(G.dO, q, n); copyD(G.dT, q + n, n); copyD(G.hO, q + 2 * n, n); copyD(G.hT, q + 3 * n, n);
+            copyD(G.mac, q + 4 * n, 3 * n); copyD(G.tv, q + 7 * n, 8 * n);
+            copyD(G.dualO, q + 15 * n, 3 * n); copyD(G.dualT, q + 18 * n, 3 * n);
+        }
+    }
+    void tapeStart(int every) {
+        requireFrozen("astg_tape_start");
+        if (every < 0) throw std::invalid_argument("astg_tape_start: checkpoint_every must be >= 0");
+        freeTape();
+        T.on = true;
+        T.every = every;
+    }
+    // records the step about to run; returns where its advection input goes (store mode)
+    double* tapeBeforeStep(double dt) {
+        int k = T.steps;
+        if (T.every > 0 && k % T.every == 0) {
+            size_t j = (size_t)(k / T.every);
+            if (T.ckpt.size() <= j) T.ckpt.push_back(tapeAlloc(FULL_DOUBLES));
+            saveFull(T.ckpt[j]);
+            T.ckCur.push_back(cur);
+            T.ckFirst.push_back(firstSource ? 1 : 0);
+        }
+        T.dt.push_back(dt);
+        T.first.push_back(firstSource ? 1 : 0);
+        if (T.every > 0) return nullptr;
+        if (T.adv.size() <= (size_t)k) T.adv.push_back(tapeAlloc(ADV_DOUBLES));
+        return T.adv[k];
+    }
+    // the step transposes for taped step k, whose advection input is at adv
+    void adjStep(int k, double* adv) {
+        double dt = T.dt[k];
+        Fields C = advectionView(adv);
+        adjStage(5, dt, C, false);
+        const Fields& Fr = F[cur];
+        for (int i = 4; i >= 0; --i) adjStage(i, dt, Fr, T.first[k] != 0);
+    }
+    // reverse pass over every taped step: GA[ga] holds the cotangent of the final state on entry
+    // and that of the state at astg_tape_start on return; source gradients accumulate
+    void backward(astg_adjoint_stats* out) {
+        if (!T.on || T.steps == 0) throw std::invalid_argument("astg_backward: no taped steps");
+        allocAdjoint();
+        adjustFrozen();
+        int n = T.steps;
+        if (!T.endState) T.endState = tapeAlloc(FULL_DOUBLES);
+        saveFull(T.endState);
+        int endCur = cur;
+        bool endFirst = firstSource;
+        astg_solve_stats endLast = last;
+        adjSolves = adjIters = 0;
+        adjN = -1;
+        int recomputed = 0;
+        float msRe = 0;
+        T.recording = 0;
+        cudaEvent_t e0, e1, r0, r1;
+        cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&r0); cudaEventCreate(&r1);
+        ck(cudaEventRecord(e0, st), "event");
+        try {
+            if (T.every <= 0) {
+                for (int k = n - 1; k >= 0; --k) adjStep(k, T.adv[k]);
+            } else {
+                int K = T.every;
+                while ((int)T.adv.size() < std::min(K, n)) T.adv.push_back(tapeAlloc(ADV_DOUBLES));
+                int nseg = (n + K - 1) / K;
+                for (int j = nseg - 1; j >= 0; --j) {
+                    int a = j * K, b = std::min(n, a + K);
+                    restoreFull(T.ckpt[j]);
+                    cur = T.ckCur[j];
+                    firstSource = T.ckFirst[j] != 0;
+                    ck(cudaEventRecord(r0, st), "event");
+                    for (int k = a; k < b; ++k) {
+                        advTarget = T.adv[k - a];
+                        step(T.dt[k], nullptr);
+                        ++recomputed;
+                    }
+                    advTarget = nullptr;
+                    ck(cudaEventRecord(r1, st), "event");
+                    ck(cudaEventSynchronize(r1), "sync");
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, r0, r1);
+                    msRe += ms;
+                    adjN = -1;  // the recomputed steps re-assembled the same matrix; factor once more
+                    for (int k = b - 1; k >= a; --k) adjStep(k, T.adv[k - a]);
+                }
+            }
+        } catch (...) {
+            advTarget = nullptr;
+            T.recording = 1;
+            restoreFull(T.endState);
+            cur = endCur;
+            firstSource = endFirst;
+            last = endLast;
+            cudaStreamSynchronize(st);
+            for (cudaEvent_t e : {e0, e1, r0, r1}) cudaEventDestroy(e);
+            throw;
+        }
+        ck(cudaEventRecord(e1, st), "event");
+        restoreFull(T.endState);
+        cur = endCur;
+        firstSource = endFirst;
+        last = endLast;
+        T.recording = 1;
+        checkStatus();
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        for (cudaEvent_t e : {e0, e1, r0, r1}) cudaEventDestroy(e);
+        if (out) {
+            out->steps = n;
+            out->checkpoints = (int)T.ckCur.size();
+            out->recomputed_steps = recomputed;
+            out->solves = (int)adjSolves;
+            out->pcg_iterations = adjIters;
+            out->ms = ms;
+            out->ms_recompute = msRe;
+            out->tape_bytes = T.bytes;
+        }
+    }
+    // VJP of one step at the current state, which is left as it is
+    void stepVjp(double dt) {
+        requireFrozen("astg_step_vjp");
+        allocAdjoint();
+        adjustFrozen();
+        if (T.on && T.recording) throw std::invalid_argument("astg_step_vjp: not while a tape is recording");
+        double* full = rawAlloc(FULL_DOUBLES);
+        double* adv = nullptr;
+        try {
+            adv = rawAlloc(ADV_DOUBLES);
+        } catch (...) {
+            cudaFree(full);
+            throw;
+        }
+        int c0 = cur;
+        bool f0 = firstSource;
+        astg_solve_stats l0 = last;
+        try {
+            saveFull(full);
+            for (int i = 0; i < 5; ++i) stage(i, dt);
+            saveAdvectionInput(adv);
+            restoreFull(full);
+            cur = c0;
+            firstSource = f0;
+            last = l0;
+            adjN = -1;
+            Fields C = advectionView(adv);
+            adjStage(5, dt, C, false);
+            for (int i = 4; i >= 0; --i) adjStage(i, dt, F[cur], f0);
+            checkStatus();
+        } catch (...) {
+            cudaStreamSynchronize(st);
+            cudaFree(full);
+            cudaFree(adv);
+            throw;
+        }
+        ck(cudaStreamSynchronize(st), "sync");
+        cudaFree(full);
+        cudaFree(adv);
+    }
+
     // ---------------------------------------------------------------- array exchange
     // "t_<field>" addresses the swap partner of a double-buffered state array
     static bool isPartner(const std::string& n) {
@@ -1159,14 +1535,15 @@ struct astg_handle {
             if (n.compare(2, std::string::npos, f) == 0) return true;
         return false;
     }
+    // the caller's buffer may be host or device memory (unified addressing)
     template <class T>
     void down(const T* src, void* dst, size_t n) {
-        ck(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, st), "download");
+        ck(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDefault, st), "download");
         ck(cudaStreamSynchronize(st), "download");
     }
     template <class T>
     void up(T* dst, const void* src, size_t n) {
-        ck(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDefault, st), "upload");
         ck(cudaStreamSynchronize(st), "upload");
     }
     int lastN() {
@@ -1175,8 +1552,36 @@ struct astg_handle {
         return n;
     }
 
+    // "adj_<field>": the cotangent arrays of the adjoint (f64, same shapes as the state arrays)
+    double* adjArray(const std::string& name, size_t* n) {
+        if (name.compare(0, 4, "adj_") != 0) return nullptr;
+        allocAdjoint();
+        std::string f = name.substr(4);
+        Fields& g = GA[ga];
+        size_t S1 = (size_t)S;
+        if (f == "density_oct") { *n = S1; return g.dO; }
+        if (f == "density_tilt") { *n = S1; return g.dT; }
+        if (f == "heat_oct") { *n = S1; return g.hO; }
+        if (f == "heat_tilt") { *n = S1; return g.hT; }
+        if (f == "mac") { *n = 3 * S1; return g.mac; }
+        if (f == "tilt_vel") { *n = 8 * S1; return g.tv; }
+        if (f == "dual_oct") { *n = 3 * S1; return g.dualO; }
+        if (f == "dual_tilt") { *n = 3 * S1; return g.dualT; }
+        if (f == "source_density_oct") { *n = S1; return dGsO; }
+        if (f == "source_density_tilt") { *n = S1; return dGsT; }
+        throw std::invalid_argument("unknown adjoint array " + name);
+    }
+
     // returns the byte size of a named array; copies it out when dst != nullptr
     size_t getArray(const std::string& name0, void* dst, size_t bytes) {
+        {
+            size_t n = 0;
+            if (double* a = adjArray(name0, &n)) {
+                if (dst && bytes != 8 * n) throw std::invalid_argument("astg_get " + name0 + ": expected " + std::to_string(8 * n) + " bytes");
+                if (dst) down(a, dst, n);
+                return 8 * n;
+            }
+        }
         std::string name = name0;
         int b = cur;
         if (isPartner(name)) { b = 1 - cur; name = name.substr(2); }
@@ -1216,6 +1621,8 @@ struct astg_handle {
             return nb;
         }
         if (b != cur) throw std::invalid_argument("astg_get: no swap partner for " + name);
+        if (name == "source_density_oct") { size_t nb = need(8 * (size_t)S); if (dst) down(dSrcO, dst, S); return nb; }
+        if (name == "source_density_tilt") { size_t nb = need(8 * (size_t)S); if (dst) down(dSrcT, dst, S); return nb; }
         if (name == "slot_coords") {
             size_t nb = need(16 * (size_t)S);
             if (dst) {
@@ -1287,6 +1694,14 @@ struct astg_handle {
     }
 
     void setArray(const std::string& name0, const void* src, size_t bytes) {
+        {
+            size_t n = 0;
+            if (double* a = adjArray(name0, &n)) {
+                if (bytes != 8 * n) throw std::invalid_argument("astg_set " + name0 + ": expected " + std::to_string(8 * n) + " bytes");
+                up(a, src, n);
+                return;
+            }
+        }
         std::string name = name0;
         int b = cur;
         if (isPartner(name)) { b = 1 - cur; name = name.substr(2); }
@@ -1311,6 +1726,8 @@ struct astg_handle {
             up(G.tf, v.data(), S);
             return;
         }
+        if (b == cur && name == "source_density_oct") { need(8 * (size_t)S); up(dSrcO, src, S); return; }
+        if (b == cur && name == "source_density_tilt") { need(8 * (size_t)S); up(dSrcT, src, S); return; }
         if (name == "tilt_open") {
             need((size_t)S);
             const uint8_t* q = (const uint8_t*)src;
@@ -1415,6 +1832,7 @@ astg_status astg_step(astg_handle* h, double dt, astg_step_stats* stats) {
 
 astg_status astg_stage(astg_handle* h, int stage, double dt) {
     return guard(h, [&] {
+        if (h->T.on && h->T.recording) throw std::invalid_argument("astg_stage: a tape is recording (use astg_step)");
         h->stage(stage, dt);
         h->checkStatus();
     });
@@ -1485,6 +1903,70 @@ astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32
     astg_status s = guard(h, [&] { h->solveExternal(n, rowptr, col, val, b, x, rel_tol, max_iter, prec, stats); });
     if (s == ASTG_OK && !h->last.converged) return ASTG_NOT_CONVERGED;
     return s;
+}
+
+astg_status astg_set_tilt_adaptivity(astg_handle* h, int on) {
+    return guard(h, [&] {
+        if (h->T.on && h->T.recording && on) throw std::invalid_argument("astg_set_tilt_adaptivity: a tape is recording");
+        h->P.tilt_adaptivity = on != 0;
+        if (!on) {
+            // freeze: both buffers carry the current tilt-E state from now on
+            const Fields& C = h->F[h->cur];
+            Fields& N = h->F[1 - h->cur];
+            h->copyD(N.te, C.te, (size_t)h->S);
+            ck(cudaMemcpyAsync(N.tf, C.tf, sizeof(uint32_t) * (size_t)h->S, cudaMemcpyDeviceToDevice, h->st), "copy");
+            ck(cudaStreamSynchronize(h->st), "sync");
+        }
+    });
+}
+
+astg_status astg_tape_start(astg_handle* h, int checkpoint_every) {
+    return guard(h, [&] { h->tapeStart(checkpoint_every); });
+}
+
+astg_status astg_tape_stop(astg_handle* h) {
+    return guard(h, [&] { h->freeTape(); });
+}
+
+astg_status astg_adjoint_reset(astg_handle* h) {
+    return guard(h, [&] { h->resetAdjoint(); });
+}
+
+astg_status astg_backward(astg_handle* h, astg_adjoint_stats* stats) {
+    return guard(h, [&] { h->backward(stats); });
+}
+
+astg_status astg_stage_vjp(astg_handle* h, int stage, double dt) {
+    if (!(dt > 0)) return ASTG_BAD_ARG;
+    return guard(h, [&] { h->stageVjp(stage, dt); });
+}
+
+astg_status astg_step_vjp(astg_handle* h, double dt) {
+    if (!(dt > 0)) return ASTG_BAD_ARG;
+    return guard(h, [&] { h->stepVjp(dt); });
+}
+
+astg_status astg_adjoint_probe(astg_handle* h, int what, int n, const double* pos, double* out) {
+    if (!h || (what != 0 && what != 1) || n < 0 || (n > 0 && (!pos || !out))) return ASTG_BAD_ARG;
+    return guard(h, [&] {
+        if (n == 0) return;
+        size_t per = what == 0 ? 5 : 15;
+        double* dp = nullptr;
+        double* dout = nullptr;
+        ck(cudaMalloc(&dp, 24 * (size_t)n), "cudaMalloc");
+        if (cudaMalloc(&dout, 8 * per * (size_t)n) != cudaSuccess) {
+            cudaFree(dp);
+            throw CudaError("cudaMalloc");
+        }
+        cudaError_t e = cudaMemcpyAsync(dp, pos, 24 * (size_t)n, cudaMemcpyDefault, h->st);
+        if (e == cudaSuccess) e = astg::launch_adj_probe(h->d, h->F[h->cur], what, n, dp, dout, h->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, 8 * per * (size_t)n, cudaMemcpyDefault, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        cudaFree(dp);
+        cudaFree(dout);
+        ck(e, "adjoint probe");
+        h->checkStatus();
+    });
 }
 
 astg_status astg_max_velocity(astg_handle* h, double* out) {

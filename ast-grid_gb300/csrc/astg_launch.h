@@ -195,4 +195,26 @@ size_t extrapolate_scratch_bytes(int S);
 long long launch_extrapolate(const Dev& d, const Fields& F, double* oct, double* til, const double* sdf, int sres,
                              double offset, double maxFactor, void* scratch, int* passes, cudaStream_t st);
 
+// ---------------------------------------------------------------- adjoint (astg_adjoint.cu)
+// Transposes of the step's stages with the topology frozen.  F supplies the frozen tilt-E state
+// (te, tf) and, for the advection, the field values of the stage's input state; G holds
+// cotangents in the Fields layout and is updated in place from the cotangent of the stage's output
+// to that of its input.
+cudaError_t launch_adj_probe(const Dev& d, const Fields& F, int what, int n, const double* pos, double* out, cudaStream_t st);
+void launch_adj_owners(const Dev& d, const double* te, int* ownJ, int* ownH, cudaStream_t st);
+void launch_adj_source(const Dev& d, const Fields& G, double* gsO, double* gsT, cudaStream_t st);
+void launch_adj_scalar_ghost(const Dev& d, double* go, double* gt, const double* te, const uint32_t* tf, const int* ownJ,
+                             const int* ownH, cudaStream_t st);
+void launch_adj_force(const Dev& d, const Fields& F, const Fields& G, const uint8_t* open, double dt, double* gamb,
+                      double invCount, cudaStream_t st);
+void launch_adj_walls_and_ghost(const Dev& d, const Fields& F, const Fields& G, const uint8_t* lastWriter, cudaStream_t st);
+void launch_adj_pressure_update(const Dev& d, const Fields& F, const Fields& G, const uint8_t* open, const int* pO,
+                                const int* pT, double* gp, double dt, cudaStream_t st);
+void launch_adj_rhs(const Dev& d, const Fields& F, const Fields& G, const uint8_t* open, const Proj& P, const int* hoPtr,
+                    const int* hoIdx, const double* lam, double scale, cudaStream_t st);
+void launch_adj_dual(const Dev& d, const Fields& F, const Fields& G, const int* ownJ, const int* ownH, cudaStream_t st);
+// GN: cotangent of the state after the step (consumed); GC: cotangent of the advected-from state C
+void launch_adj_advect(const Dev& d, const Fields& C, const Fields& GC, const Fields& GN, const uint8_t* open, double dt,
+                       const int* ownJ, const int* ownH, cudaStream_t st);
+
 }  // namespace astg

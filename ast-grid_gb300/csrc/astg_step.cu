@@ -21,14 +21,15 @@ ASTG_HD inline bool in_src(const Dev& d, V3 p) {
 ASTG_HD inline bool ghost(const Dev& d, int s) { return slot_f(d, s) & SF_GHOST; }
 
 // ------------------------------------------------------------------ source
-// example/octree_smoke_3d/main.cpp:23-86 with density = heat = 1 and an upward velocity of 1
+// example/octree_smoke_3d/main.cpp:23-86 with heat = 1, an upward velocity of 1 and the density
+// of each slot's source (1 unless set as a differentiable parameter)
 __global__ void k_source_slots(Dev d, Fields F) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.S || ghost(d, s)) return;
-    if (in_src(d, cell_pos(d, s))) { F.dO[s] = 1; F.hO[s] = 1; }
+    if (in_src(d, cell_pos(d, s))) { F.dO[s] = d.srcO[s]; F.hO[s] = 1; }
     V3 vp = vert_pos(d, s);
     if (in_src(d, vp)) {
-        F.dT[s] = 1;
+        F.dT[s] = d.srcT[s];
         F.hT[s] = 1;
         for (int k = 0; k < 8; ++k) F.tv[(size_t)s * 8 + k] = 1.0 * INV_SQRT3;
     }
@@ -40,7 +41,7 @@ __global__ void k_source_half(Dev d, Fields F) {
     int hs = d.half[i];
     V3 vp = vert_pos(d, hs);
     if (!in_src(d, vp)) return;
-    F.dT[hs] = 1;
+    F.dT[hs] = d.srcT[hs];
     F.hT[hs] = 1;
     int dir = tf_dir(F.tf[hs]);
     double nv[8] = {0, 0, 0, 0, 0, 0, 0, 0};

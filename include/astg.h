@@ -122,6 +122,7 @@ long long astg_size(const astg_handle* h, int what);
  *   tilt_vel (f64, slots x 8)  dual_oct dual_tilt (f64, slots x 3)
  *   tilt_flags (i32, slots x 2: bit 0 largest, 1 closed, 2 fixed, 3 T-joint, 4 closed by T-joint,
  *   5 half tilt; half direction)  tilt_open (u8, slots: bit 0 open, bit 1 fixed)
+ *   source_density_oct source_density_tilt (f64, slots: density the source sets, default 1)
  *   prefix "t_" = the swap-partner buffer of the reference's double-buffered grids;
  * read only: slot_coords (i32, slots x 4: x y z flags) level_sizes (i32, levels x 3)
  *   half_tilts t_joints closed_by_half_tilt (i64 packed level coordinates) split_map (i32)
@@ -205,6 +206,63 @@ astg_status astg_extrapolate(astg_handle* h, const char* field, const double* sd
  * and must be serialised by the caller. */
 astg_status astg_mean_temperature_noalloc(const double* d_heat_oct, const int64_t* level_slots, int levels,
                                           double* d_amb, void* stream, char* err, size_t errlen);
+
+/* ---------------------------------------------------------------- reverse mode (adjoint)
+ * No counterpart in the reference, which has no gradients: the transposes of the step's stages for a
+ * window of steps with the octree topology frozen (astg_params.tilt_adaptivity = 0, so the tilt-E
+ * state, the DOF map and the pressure matrix stay fixed).  The advection transpose is the transposed
+ * octree interpolation (scattered with atomics) plus the chain through the RK2 back-trace; the
+ * projection transpose is one solve with the same SPD matrix (MIC(0)-PCG, the precision and
+ * tolerance of astg_set_precision / astg_set_solver_parameters).
+ * Cotangents are exchanged through astg_get / astg_set under the names
+ *   adj_density_oct adj_density_tilt adj_heat_oct adj_heat_tilt adj_mac adj_tilt_vel adj_dual_oct
+ *   adj_dual_tilt (f64, the shapes of the state arrays) and adj_source_density_oct /
+ *   adj_source_density_tilt (f64, slots: gradients of the per-slot source densities
+ *   "source_density_oct" / "source_density_tilt", which default to 1). */
+typedef struct astg_adjoint_stats {
+    int steps;              /* taped steps differentiated */
+    int checkpoints;        /* checkpoints held (0 when every step's advection input was kept) */
+    int recomputed_steps;   /* forward steps re-run from checkpoints during the pass */
+    int solves;             /* adjoint pressure solves */
+    long long pcg_iterations;  /* their PCG iterations (inner iterations for ASTG_MIXED) */
+    double ms;              /* device time of the whole reverse pass (CUDA events) */
+    double ms_recompute;    /* of which re-running forward steps */
+    long long tape_bytes;   /* device memory held by the tape */
+} astg_adjoint_stats;
+
+/* enableTiltAdaptivity (include/octree_omnigrid_solver3.h:23-57, read in advect,
+ * src/octree_omnigrid_solver3.cpp:852).  Turning it off also copies the current tilt-E state into the
+ * swap-partner buffer, so the octree topology stays frozen from here on (the reference swaps the two
+ * tilt-E buffers every step, which with the flag cleared mid-run would alternate between them). */
+astg_status astg_set_tilt_adaptivity(astg_handle* h, int on);
+
+/* Starts recording the astg_step calls that follow (any earlier tape is dropped).  checkpoint_every
+ * = 0 keeps each step's advection input (13 doubles per slot per step); k > 0 keeps the whole state
+ * every k steps (42 doubles per slot) and re-runs the steps of each segment during astg_backward.
+ * ASTG_BAD_ARG when tilt adaptivity is on.  astg_stage is refused while recording. */
+astg_status astg_tape_start(astg_handle* h, int checkpoint_every);
+astg_status astg_tape_stop(astg_handle* h);  /* frees the tape */
+
+/* Zeroes every cotangent array, source gradients included. */
+astg_status astg_adjoint_reset(astg_handle* h);
+
+/* Reverse pass over all taped steps.  On entry the adj_* state arrays hold the cotangent of the
+ * final state (e.g. d loss / d density_oct); on return they hold the cotangent of the state at
+ * astg_tape_start, and adj_source_density_* has the source gradients added.  The forward state is
+ * left at the final state; the tape stays, so the pass can be repeated with another cotangent. */
+astg_status astg_backward(astg_handle* h, astg_adjoint_stats* stats);
+
+/* Vector-Jacobian product of one step (astg_step_vjp) or one stage (astg_stage_vjp, stages as in
+ * astg_stage) at the current state, which is left unchanged: the adj_* arrays go from the cotangent
+ * of the output to that of the input. */
+astg_status astg_step_vjp(astg_handle* h, double dt);
+astg_status astg_stage_vjp(astg_handle* h, int stage, double dt);
+
+/* The samplers' weight enumeration used by the transposes, at n positions (xyz, host or device
+ * memory) of the current state: what 0 -> per point {scalar sample of density, the same from the
+ * weights, its gradient (3)}; what 1 -> {velocity sample (3), from the weights (3), Jacobian (9,
+ * row c = d v_c / d p)}. */
+astg_status astg_adjoint_probe(astg_handle* h, int what, int n, const double* pos, double* out);
 
 #ifdef __cplusplus
 }
