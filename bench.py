@@ -235,6 +235,80 @@ def isolated_solves(args, device):
     return res
 
 
+def adjoint_window(args, device):
+    """Reverse mode at scale: 64^3 coarsest cells, 2 levels (128^3-equivalent), tilts opened by 4
+    adaptive steps and then frozen, `adjoint_steps` steps taped with a checkpoint every
+    `adjoint_every` steps (the others recomputed during the reverse pass).  Loss = ||density - g||_2
+    over the octagon cells (volume-weighted; g a Gaussian blob at (0.5, 0.5, 0.6) z-up, sigma 0.1,
+    peak 1); gradients with respect to the initial face velocities and the per-slot source densities.
+    Run in the mixed form (FP32 inner PCG in both the forward and the adjoint solves) and in FP64 on
+    the same window; the FP64 gradient is the reference for the mixed one.  Times are device times:
+    forward = the taped steps (checkpoint copies included), backward = astg_backward."""
+    import numpy as np
+    import torch
+
+    import ast_solver
+
+    free0 = torch.cuda.mem_get_info(device)[0]
+    s = ast_solver.OctreeSmoke3(64, 2, device=device)
+    for _ in range(4):
+        s.update(DT)
+    s.set_tilt_adaptivity(False)
+    names = ["density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt"]
+    X = {k: s.get(k) for k in names}
+    Pt = {k: s.get("t_" + k) for k in names}
+    coords, sizes = s.get("slot_coords"), s.get("level_sizes")
+    lev = np.repeat(np.arange(len(sizes)), sizes[:, 2])
+    res0 = s.size(2)
+    h = (1.0 / res0) * (2.0 ** lev)
+    cells = ((coords[:, 3] & 2) == 0) & np.all(coords[:, :3] < ((res0 >> lev) - 1)[:, None], axis=1)
+    centre = (coords[:, :3] + 0.5) * h[:, None]
+    g = np.exp(-((centre - np.array([0.5, 0.5, 0.6])) ** 2).sum(1) / (2 * 0.1 ** 2))
+    w = np.where(cells, h ** 3, 0.0)
+    peak_used = 0
+
+    def run(prec):
+        nonlocal peak_used
+        for k, v in X.items():
+            s.set(k, v)
+        for k, v in Pt.items():
+            s.set("t_" + k, v)
+        s.set_precision(prec)
+        s.tape_start(args.adjoint_every)
+        fwd = 0.0
+        for _ in range(args.adjoint_steps):
+            s.update(DT)
+            fwd += s.last_step.ms_total
+        r = s.get("density_oct") - g
+        loss = float(np.sqrt((w * r * r).sum()))
+        s.adjoint_reset()
+        s.set("adj_density_oct", w * r / loss)
+        st = s.backward()
+        peak_used = max(peak_used, free0 - torch.cuda.mem_get_info(device)[0])
+        grads = [s.get("adj_mac"), s.get("adj_tilt_vel"), s.get("adj_source_density_oct"),
+                 s.get("adj_source_density_tilt")]
+        s.tape_stop()
+        return {"loss": loss, "forward_ms": fwd, "backward_ms": st.ms, "recompute_ms": st.ms_recompute,
+                "ratio": st.ms / fwd, "adjoint_pcg_iters_mean": st.pcg_iterations / max(st.solves, 1),
+                "checkpoints": st.checkpoints, "recomputed_steps": st.recomputed_steps,
+                "tape_bytes": st.tape_bytes}, grads
+
+    mixed, gm = run("mixed")
+    fp64, g64 = run("fp64")
+    num = np.sqrt(sum(((a - b) ** 2).sum() for a, b in zip(gm, g64)))
+    den = np.sqrt(sum((b * b).sum() for b in g64))
+    out = {"config": f"64^3 coarsest x 2 levels (128^3-equivalent), {args.adjoint_steps} steps, checkpoint "
+                     f"every {args.adjoint_every} with recompute, topology frozen after 4 adaptive steps; "
+                     "loss ||density - g||_2; gradients w.r.t. initial faces and source densities",
+           "slots": s.slots, "mixed": mixed, "fp64": fp64,
+           "adjoint_fwd_cost_ratio": mixed["ratio"],
+           "grad_rel_error_mixed_vs_fp64": float(num / den),
+           "peak_device_bytes": int(peak_used),
+           "fields": "FP64 fields; the mixed form runs the forward and adjoint PCG with FP32 inner iterations"}
+    s.close()
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if ws > 1 and rank != 0:
@@ -410,6 +484,9 @@ def run_ours(args):
     solves = None
     if rank == 0 and args.solve_rhs > 0:
         solves = isolated_solves(args, local)
+    adjoint = None
+    if rank == 0 and args.adjoint_steps > 0:
+        adjoint = adjoint_window(args, local)
 
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
@@ -420,7 +497,7 @@ def run_ours(args):
             "pcg_ms_per_solve": float(np.mean(pcg_ms)), "pcg_iters_mean": float(np.mean(iters)), "mixed": mixed,
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "roofline": roofline, "kernels": kernel_breakdown, "cpu_baseline": cpu, "e2e": e2e,
-            "clocks": clocks, "gpu_launches": launches, "isolated_solves": solves}
+            "clocks": clocks, "gpu_launches": launches, "isolated_solves": solves, "adjoint": adjoint}
     s.close()
     D.barrier()
     if rank == 0:
@@ -440,6 +517,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20, help="steps of the end-to-end loop (at most --steps)")
     ap.add_argument("--solve-steps", type=int, default=100, help="steps before the isolated solves")
     ap.add_argument("--solve-rhs", type=int, default=20, help="right-hand sides of the isolated solves (0: skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=128, help="steps of the differentiated window (0: skip)")
+    ap.add_argument("--adjoint-every", type=int, default=16, help="checkpoint interval of the adjoint tape")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
