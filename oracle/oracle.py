@@ -85,8 +85,9 @@ class Oracle:
     def __init__(self, coarsest, levels, tol=1e-6, buoy_d=-0.1, buoy_t=1.0, decay=1.0, rho=2.0, noise=1e-3,
                  source=(0.5, 0.5, 0.12, 0.06), seed=0, max_iter=3000, tilt_adaptivity=True, closed_mask=47,
                  reduce_mode=0, ref_workers=8, openmp=False):
-        """reduce_mode 0 follows the reference's own reduction order (Eigen's dot, per-worker
-        partial sums over ref_workers workers); 1 follows the CUDA library's fixed tree."""
+        """reduce_mode 0 follows the reference's own arithmetic order (Eigen's dot, per-worker
+        partial sums over ref_workers workers); 1 follows the CUDA library's (its fixed reduction
+        tree, and one fused multiply-subtract per update of the MIC(0) sweeps)."""
         p = _Params(tol, buoy_d, buoy_t, decay, rho, noise, source[0], source[1], source[2], source[3], seed,
                     max_iter, 1 if tilt_adaptivity else 0, closed_mask, reduce_mode, ref_workers)
         self._lib = lib(openmp)

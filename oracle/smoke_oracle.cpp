@@ -148,7 +148,8 @@ struct Params {
     //      (include/pcgsolver/blas_wrapper.h:101-110 over ThreadPool::parallelForPlainTF,
     //      include/thread_pool.h:319-348) with refWorkers workers;
     //  1 = the fixed reduction tree of the CUDA library (chunks of 2048, 256 lanes x 8
-    //      strided elements, binary tree over the lanes, chunk partials reduced the same way).
+    //      strided elements, binary tree over the lanes, chunk partials reduced the same way),
+    //      and the library's MIC(0) sweeps: each update one fused multiply-subtract.
     int reduceMode = 0;
     int refWorkers = 8;
 };
@@ -1545,15 +1546,22 @@ public:
             }
         }
     }
-    // :211-253
+    // :211-253.  reduce_mode 0: the reference's multiply-then-subtract; reduce_mode 1 (the GPU
+    // library's order): each update as one fused multiply-subtract, std::fma(-L, z, acc), in the
+    // same order (correctly rounded, the same operation as the GPU's FP64 fma)
     void applyPrecond(const std::vector<double>& r, std::vector<double>& z) {
         z = r;
+        const bool fused = P.reduceMode != 0;
         for (int i = 0; i < F.n; ++i) {
             z[i] *= F.invdiag[i];
-            for (int j = F.colstart[i]; j < F.colstart[i + 1]; ++j) z[F.rowindex[j]] -= F.value[j] * z[i];
+            for (int j = F.colstart[i]; j < F.colstart[i + 1]; ++j) {
+                double& t = z[F.rowindex[j]];
+                t = fused ? std::fma(-F.value[j], z[i], t) : t - F.value[j] * z[i];
+            }
         }
         for (int i = F.n - 1; i >= 0; --i) {
-            for (int j = F.colstart[i]; j < F.colstart[i + 1]; ++j) z[i] -= F.value[j] * z[F.rowindex[j]];
+            for (int j = F.colstart[i]; j < F.colstart[i + 1]; ++j)
+                z[i] = fused ? std::fma(-F.value[j], z[F.rowindex[j]], z[i]) : z[i] - F.value[j] * z[F.rowindex[j]];
             z[i] *= F.invdiag[i];
         }
     }
