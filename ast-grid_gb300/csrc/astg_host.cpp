@@ -631,6 +631,10 @@ struct astg_handle {
         J.invdiag = dalloc<double>(rows);
         J.adiag = dalloc<double>(rows);
         J.ready = dalloc<int>(rows);
+        J.planPtr = dalloc<int>(rows * ROW_W + 1);
+        J.planCap = rows * ROW_W * 2;
+        J.plan = dalloc<int>(J.planCap);
+        J.planTotal = dalloc<int>(1);
         J.counter = dalloc<int>(1);
         J.level = dalloc<int>(rows);
         J.levelCnt = dalloc<int>(rows + 1);
@@ -659,7 +663,7 @@ struct astg_handle {
         J.pcActive = 0;
         J.pcSmem = 0;
         J.pcLgBlock = 8;  // 256-row ownership blocks (measured: 64 to 4096 within 3 %)
-        long long scanMax = std::max(rows + 1, (long long)std::max(J.pcCluster, 1) * (rows + 1));
+        long long scanMax = std::max(rows * ROW_W + 1, (long long)std::max(J.pcCluster, 1) * (rows + 1));
         J.bsum = dalloc<int>((scanMax + 1023) / 1024 + 1);
         if (J.pcCluster && J.pcAsync) {
             J.chunk = dalloc<int>(1);

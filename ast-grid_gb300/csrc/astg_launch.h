@@ -69,6 +69,13 @@ struct Proj {
     double* invdiag;
     double* adiag;
     int* ready;      // rows, epoch flags
+    // pattern-only plan of the factorisation: for lower entry q of row j (column k), one code per
+    // upper entry of row k (k's column of L), in order: 0 nothing, 1 missing, 2 diagonal,
+    // (bb - first upper entry of row j) << 2 | 3 matched entry bb
+    int* planPtr;    // nnz capacity + 1
+    int* plan;
+    long long planCap;
+    int* planTotal;  // device scalar
     int* counter;
     int sweepBlocks;
     // level schedule of the lower factor (rows grouped by dependency depth), rebuilt per solve

@@ -1719,12 +1719,135 @@ static void precond(const Dev& d, Proj& P, const double* r, double* z, int& epoc
     prof_end(prof, st);
 }
 
+// ---- the factorisation with its merge plan computed first.  What k_mic_factor works out per
+// (column j, earlier column k) while it waits on the chain -- which of k's entries are missing
+// from j's pattern, which one is the diagonal, which entry of j each matched one updates -- depends
+// on the pattern only, so one parallel pass records it and the chained pass only applies it: the
+// same updates in the same order (bit-identical), with the loads of k's values independent of
+// one another once k is ready.
+enum { PLAN_NONE = 0, PLAN_MISSING = 1, PLAN_DIAG = 2, PLAN_MATCH = 3 };
+__global__ void k_plan_count(Proj P, int* cnt) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *P.nDof) return;
+    for (int q = P.rowPtr[j]; q < P.rowPtr[j + 1]; ++q) {
+        int k = P.col[q];
+        cnt[q] = (k < j && P.adiag[k] != 0) ? P.rowPtr[k + 1] - (P.diagPos[k] + 1) : 0;
+    }
+}
+__global__ void k_plan_fill(Proj P) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *P.nDof) return;
+    int rj0 = P.rowPtr[j], rj1 = P.rowPtr[j + 1];
+    int dgj = P.diagPos[j];
+    int upj = dgj >= 0 ? dgj + 1 : rj1;
+    for (int qq = rj0; qq < rj1; ++qq) {
+        int k = P.col[qq];
+        if (k >= j) break;
+        if (P.adiag[k] == 0) continue;
+        int* out = P.plan + P.planPtr[qq];
+        int a0 = P.diagPos[k] + 1, a = a0, ak = P.rowPtr[k + 1];
+        if (P.planPtr[qq] + (ak - a0) > P.planCap) return;  // checked on the host through planTotal
+        int b = rj0;
+        while (a < ak && P.col[a] < j) {
+            int code = PLAN_NONE;
+            while (b < rj1) {
+                if (P.col[b] < P.col[a]) ++b;
+                else if (P.col[b] == P.col[a]) break;
+                else { code = PLAN_MISSING; break; }
+            }
+            out[a - a0] = code;
+            ++a;
+        }
+        if (a < ak) out[a - a0] = P.col[a] == j ? PLAN_DIAG : PLAN_NONE;
+        ++a;
+        int bb = upj;
+        while (a < ak && bb < rj1) {
+            if (P.col[bb] < P.col[a]) ++bb;
+            else if (P.col[bb] == P.col[a]) { out[a - a0] = ((bb - upj) << 2) | PLAN_MATCH; ++a; ++bb; }
+            else { out[a - a0] = PLAN_MISSING; ++a; }
+        }
+        while (a < ak) { out[a - a0] = PLAN_MISSING; ++a; }
+    }
+}
+constexpr int PLAN_MAXU = 16;  // upper entries of a column applied from registers (more: in place)
+__global__ void k_mic_factor_plan(Dev d, Proj P, double omega, double minDiag, int epoch) {
+    int n = *P.nDof;
+    for (;;) {
+        int j = grab_row(P.counter);
+        if (j >= n) return;
+        int rj0 = P.rowPtr[j], rj1 = P.rowPtr[j + 1];
+        int dgj = P.diagPos[j];
+        int upj = dgj >= 0 ? dgj + 1 : rj1;
+        double invd = P.invdiag[j];
+        int lev = 0;
+        for (int qq = rj0; qq < rj1; ++qq) {
+            int k = P.col[qq];
+            if (k >= j) break;
+            const int pp = P.planPtr[qq], pe = P.planPtr[qq + 1];
+            const int a0 = P.diagPos[k] + 1;
+            const int tq = P.tpos[qq];
+            int code[PLAN_MAXU];
+            const int m = pe - pp;
+#pragma unroll
+            for (int u = 0; u < PLAN_MAXU; ++u) code[u] = u < m ? P.plan[pp + u] : PLAN_NONE;
+            wait_flag(d, P.ready + k, epoch);
+            lev = max(lev, P.level[k] + 1);
+            if (m == 0 && P.adiag[k] == 0) continue;
+            double mult = P.Lv[tq];
+            double lv[PLAN_MAXU];
+#pragma unroll
+            for (int u = 0; u < PLAN_MAXU; ++u) lv[u] = (u < m && code[u] != PLAN_NONE) ? P.Lv[a0 + u] : 0.0;
+            double missing = 0;
+#pragma unroll
+            for (int u = 0; u < PLAN_MAXU; ++u) {
+                if (u >= m) break;
+                int c = code[u] & 3;
+                if (c == PLAN_MISSING) missing += lv[u];
+                else if (c == PLAN_DIAG) invd -= mult * lv[u];
+                else if (c == PLAN_MATCH) P.Lv[upj + (code[u] >> 2)] -= mult * lv[u];
+            }
+            for (int u = PLAN_MAXU; u < m; ++u) {
+                int cu = P.plan[pp + u], c = cu & 3;
+                double v = P.Lv[a0 + u];
+                if (c == PLAN_MISSING) missing += v;
+                else if (c == PLAN_DIAG) invd -= mult * v;
+                else if (c == PLAN_MATCH) P.Lv[upj + (cu >> 2)] -= mult * v;
+            }
+            invd -= omega * mult * missing;
+        }
+        double ad = P.adiag[j];
+        if (ad != 0) {
+            if (invd < minDiag * ad) invd = 1 / sqrt(ad);
+            else invd = 1 / sqrt(invd);
+            for (int q = upj; q < rj1; ++q) P.Lv[q] *= invd;
+        }
+        P.invdiag[j] = invd;
+        P.level[j] = lev;
+        __threadfence();
+        st_flag(P.ready + j, epoch);
+    }
+}
 void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st, KProf* prof) {
     int maxRows = P.rowsCap;
     ASTG_LAUNCH(k_mic_init<<<nblk(maxRows), TB, 0, st>>>(P));
     ASTG_LAUNCH(k_reset_counter<<<1, 1, 0, st>>>(P.counter));
+    bool plan = P.plan != nullptr;
+    if (plan) {
+        // counts in place (entries past nnz stay 0), exclusive scan in place: planPtr[q] = start of
+        // entry q's codes, planPtr[nnz] = total
+        long long nz = (long long)maxRows * ROW_W;
+        cudaMemsetAsync(P.planPtr, 0, sizeof(int) * (nz + 1), st);
+        ASTG_LAUNCH(k_plan_count<<<nblk(maxRows), TB, 0, st>>>(P, P.planPtr));
+        exclusive_scan(P.planPtr, P.planPtr, P.bsum, P.planTotal, nz, st);
+        int total = 0;
+        cudaMemcpyAsync(&total, P.planTotal, sizeof total, cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
+        plan = total >= 0 && total <= P.planCap;  // a larger plan: this solve uses the direct form
+        if (plan) ASTG_LAUNCH(k_plan_fill<<<nblk(maxRows), TB, 0, st>>>(P));
+    }
     prof_begin(prof, 3, st);
-    ASTG_LAUNCH(k_mic_factor<<<P.sweepBlocks, 128, 0, st>>>(d, P, omega, minDiag, ++epoch));
+    if (plan) ASTG_LAUNCH(k_mic_factor_plan<<<P.sweepBlocks, 128, 0, st>>>(d, P, omega, minDiag, ++epoch));
+    else ASTG_LAUNCH(k_mic_factor<<<P.sweepBlocks, 128, 0, st>>>(d, P, omega, minDiag, ++epoch));
     prof_end(prof, st);
 }
 
