@@ -235,6 +235,38 @@ def isolated_solves(args, device):
     return res
 
 
+def precision_comparison(args, device):
+    """The mixed form against the FP64 form on the benchmark scene: two handles from the same
+    initial state step side by side; per step the relative L2 difference of the octagon density and
+    of the pressure, and each form's final relative residual |b - A p|_inf / |b|_inf of its solve
+    (both stop at 1e-6)."""
+    import numpy as np
+
+    import ast_solver
+
+    a = ast_solver.OctreeSmoke3(COARSEST, LEVELS, device=device)
+    b = ast_solver.OctreeSmoke3(COARSEST, LEVELS, device=device, precision="mixed")
+    dens, pres, ra, rb = [], [], [], []
+    for _ in range(args.compare_steps):
+        a.update(DT)
+        b.update(DT)
+        da, db = a.get("density_oct"), b.get("density_oct")
+        pa, pb = a.get("p"), b.get("p")
+        dens.append(float(np.linalg.norm(db - da) / max(np.linalg.norm(da), 1e-300)))
+        pres.append(float(np.linalg.norm(pb - pa) / max(np.linalg.norm(pa), 1e-300)) if len(pa) == len(pb) else None)
+        for h, out in ((a, ra), (b, rb)):
+            st = h.last_step.solve
+            out.append(st.residual / (st.tolerance / 1e-6) if st.tolerance > 0 else 0.0)
+    a.close()
+    b.close()
+    pick = lambda v: {"step1": v[0], "max": max(x for x in v if x is not None), "last": v[-1]}
+    return {"config": f"{args.compare_steps} steps of the benchmark scene from the same initial state, FP64 form vs "
+                      "mixed form (separate handles)",
+            "density_rel_l2_mixed_vs_fp64": pick(dens), "pressure_rel_l2_mixed_vs_fp64": pick(pres),
+            "rel_residual_fp64": pick(ra), "rel_residual_mixed": pick(rb),
+            "per_step_density": dens}
+
+
 def adjoint_window(args, device):
     """Reverse mode at scale: 64^3 coarsest cells, 2 levels (128^3-equivalent), tilts opened by 4
     adaptive steps and then frozen, `adjoint_steps` steps taped with a checkpoint every
@@ -487,6 +519,9 @@ def run_ours(args):
     adjoint = None
     if rank == 0 and args.adjoint_steps > 0:
         adjoint = adjoint_window(args, local)
+    comparison = None
+    if rank == 0 and args.compare_steps > 0:
+        comparison = precision_comparison(args, local)
 
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
@@ -497,7 +532,8 @@ def run_ours(args):
             "pcg_ms_per_solve": float(np.mean(pcg_ms)), "pcg_iters_mean": float(np.mean(iters)), "mixed": mixed,
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "roofline": roofline, "kernels": kernel_breakdown, "cpu_baseline": cpu, "e2e": e2e,
-            "clocks": clocks, "gpu_launches": launches, "isolated_solves": solves, "adjoint": adjoint}
+            "clocks": clocks, "gpu_launches": launches, "isolated_solves": solves, "adjoint": adjoint,
+            "precision_comparison": comparison}
     s.close()
     D.barrier()
     if rank == 0:
@@ -519,6 +555,7 @@ def main():
     ap.add_argument("--solve-rhs", type=int, default=20, help="right-hand sides of the isolated solves (0: skip)")
     ap.add_argument("--adjoint-steps", type=int, default=128, help="steps of the differentiated window (0: skip)")
     ap.add_argument("--adjoint-every", type=int, default=16, help="checkpoint interval of the adjoint tape")
+    ap.add_argument("--compare-steps", type=int, default=50, help="steps of the FP64 / mixed comparison (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
