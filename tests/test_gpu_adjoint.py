@@ -273,3 +273,26 @@ def test_autograd_function(window):
     for t, r in zip(p, ref):
         assert np.allclose(t.grad.cpu().numpy(), r, rtol=1e-9, atol=1e-12 * np.abs(r).max())
     s.tape_stop()
+
+
+def test_tape_refusals():
+    s = ast_solver.OctreeSmoke3(8, 2)
+    with pytest.raises(ast_solver.AstgError) as e:
+        s.tape_start(0)  # tilt adaptivity is on: the topology is not frozen
+    assert e.value.status == ast_solver.ASTG_BAD_ARG
+    s.set_tilt_adaptivity(False)
+    with pytest.raises(ast_solver.AstgError):
+        s.backward()  # nothing taped
+    s.tape_start(0)
+    s.update(DT)
+    with pytest.raises(ast_solver.AstgError):
+        s.stage(1, DT)  # single stages would not be recorded
+    with pytest.raises(ast_solver.AstgError):
+        s.set_tilt_adaptivity(True)
+    s.adjoint_reset()
+    s.set("adj_density_oct", np.ones(s.slots))
+    st = s.backward()
+    assert st.steps == 1 and st.solves == 1
+    s.tape_stop()
+    s.stage(1, DT)  # allowed again
+    s.close()

@@ -166,3 +166,41 @@ def test_full_benchmark_size_step_bit_identical_to_oracle():
     for f in ["density_oct", "heat_oct", "mac", "tilt_vel", "dual_oct", "tilt_open", "p"]:
         assert_same(f"step1/{f}", o.get(f), s.get(f))
     s.close()
+
+
+def test_config0_fifty_steps_bit_identical_to_oracle():
+    """The reference's CPU-runnable configuration (32^3 coarsest, 3 levels = 128^3-equivalent) for
+    its full 50 steps: state, DOF map, pressure and PCG iterations identical after every step."""
+    from oracle.oracle import Oracle
+
+    s = solver(32, 3)
+    o = Oracle(32, 3, reduce_mode=1, openmp=True)
+    for k in range(50):
+        s.update(DT)
+        o.step(DT)
+        assert s.last_solve().iterations == int(o.get("pcg_iters")[0]), k
+        for f in ["density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "tilt_open", "p"]:
+            assert_same(f"step{k + 1}/{f}", o.get(f), s.get(f))
+    s.close()
+
+
+def test_mixed_form_tracks_fp64_oracle():
+    """The mixed-precision form against the FP64 oracle over 20 steps (16^3 coarsest, 3 levels):
+    per step the density within 1e-5 and the pressure within 1e-4 relative (L2), and the solve's
+    true FP64 residual at most 1e-6 |b|_inf."""
+    import numpy as np
+
+    s = solver(16, 3, precision="mixed")
+    o = oracle(16, 3)
+    for k in range(20):
+        s.update(DT)
+        o.step(DT)
+        st = s.last_step.solve
+        assert st.converged == 1 and st.outer >= 1
+        assert st.residual <= st.tolerance
+        a, b = o.get("density_oct"), s.get("density_oct")
+        assert np.linalg.norm(b - a) <= 1e-5 * np.linalg.norm(a), k
+        pa, pb = o.get("p"), s.get("p")
+        if len(pa) == len(pb):
+            assert np.linalg.norm(pb - pa) <= 1e-4 * np.linalg.norm(pa), k
+    s.close()
