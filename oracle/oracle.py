@@ -17,6 +17,8 @@ LIB = os.path.join(BUILD, "liboracle.so")
 LIB_OMP = os.path.join(BUILD, "liboracle_omp.so")  # same code, independent per-node loops on OpenMP threads
 SRC = os.path.join(HERE, "smoke_oracle.cpp")
 SCENE = os.path.join(ROOT, "ast-grid_gb300", "csrc")
+LIB2D = os.path.join(BUILD, "libast2d_oracle.so")
+SRC2D = os.path.join(HERE, "ast2d_oracle.cpp")
 
 # array names and element types exposed by orc_get
 F64 = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
@@ -32,8 +34,10 @@ SHAPES = {"mac": (3, -1), "tilt_vel": (-1, 8), "dual_oct": (-1, 3), "dual_tilt":
 
 def build(force=False, openmp=False):
     """Compile the oracle with g++ (IEEE order: no fast-math, no FP contraction).  The OpenMP
-    variant runs the reference's parallel per-node loops on threads; its results are identical."""
+    variant runs the reference's parallel per-node loops on threads; its results are identical.
+    The 2-D oracle (oracle/ast2d_oracle.cpp) is built alongside."""
     os.makedirs(BUILD, exist_ok=True)
+    build2d(force)
     out = LIB_OMP if openmp else LIB
     deps = [SRC, os.path.join(SCENE, "scene.h")]
     if not force and os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
@@ -167,3 +171,101 @@ class Oracle:
     @property
     def ndof(self):
         return self._lib.orc_size(self._h, 3)
+
+
+def build2d(force=False):
+    """Compile the 2-D oracle (uniform ASTSolver<2> restatement) with the same IEEE flags."""
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB2D) and os.path.getmtime(LIB2D) >= os.path.getmtime(SRC2D):
+        return LIB2D
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", SRC2D,
+                           "-o", LIB2D + ".tmp"])
+    os.replace(LIB2D + ".tmp", LIB2D)
+    return LIB2D
+
+
+_lib2d = None
+
+
+def lib2d():
+    global _lib2d
+    if _lib2d is None:
+        L = ctypes.CDLL(build2d())
+        L.ast2o_error.restype = ctypes.c_char_p
+        L.ast2o_create.restype = ctypes.c_void_p
+        L.ast2o_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.ast2o_destroy.argtypes = [ctypes.c_void_p]
+        L.ast2o_update.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.ast2o_stage.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
+        L.ast2o_count.restype = ctypes.c_long
+        L.ast2o_count.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+        L.ast2o_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_long]
+        L.ast2o_set.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_long]
+        L.ast2o_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_long)]
+        _lib2d = L
+    return _lib2d
+
+
+SHAPES2D = {"density_cell": "c", "heat_cell": "c", "pindex_cell": "c", "density_vert": "v", "heat_vert": "v",
+            "tilt_open": "v", "pindex_vert": "v", "mac_x": "x", "mac_y": "y", "tilt_vel": "t", "dual_vert": "d"}
+STAGES2D = {"source": 0, "force": 1, "project": 2, "advect": 3, "substep": 4}
+
+
+class Oracle2D:
+    """The uniform 2-D AST smoke solver (ASTSolver<2>, sphere source at the bottom, closed x walls,
+    open top and bottom) on an nx x ny grid of spacing dx.  reduce_mode 0 follows the reference's
+    arithmetic order (per-worker dot slices over 8 workers), 1 the CUDA library's (fixed
+    reduction tree, fused multiply-subtract in the MIC(0) sweeps)."""
+
+    def __init__(self, nx, ny, dx=None, adaptive=True, reduce_mode=0):
+        self._lib = lib2d()
+        self.nx, self.ny = nx, ny
+        self.dx = 1.0 / nx if dx is None else dx
+        self._h = self._lib.ast2o_create(nx, ny, self.dx, 1 if adaptive else 0, reduce_mode)
+        if not self._h:
+            raise ValueError(self._lib.ast2o_error().decode())
+
+    def close(self):
+        if self._h:
+            self._lib.ast2o_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(self._lib.ast2o_error().decode())
+
+    def update(self, dt):
+        """One frame: the CFL sub-stepping of Solver::update over dt."""
+        self._check(self._lib.ast2o_update(self._h, dt))
+
+    def stage(self, name, dt):
+        self._check(self._lib.ast2o_stage(self._h, STAGES2D[name], dt))
+
+    def _shape(self, name, n):
+        nx, ny = self.nx, self.ny
+        kind = SHAPES2D.get(name)
+        return {"c": (ny, nx), "v": (ny + 1, nx + 1), "x": (ny, nx + 1), "y": (ny + 1, nx),
+                "t": (ny + 1, nx + 1, 4), "d": (ny + 1, nx + 1, 2)}.get(kind, (n,))
+
+    def get(self, name):
+        kind = ctypes.c_int(0)
+        n = self._lib.ast2o_count(self._h, name.encode(), ctypes.byref(kind))
+        if n < 0:
+            raise KeyError(name)
+        out = np.empty(n, dtype=[np.float64, np.uint8, np.int32][kind.value])
+        self._check(self._lib.ast2o_get(self._h, name.encode(), out.ctypes.data, n))
+        return out.reshape(self._shape(name, n))
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.uint8 if name == "tilt_open" else np.float64).ravel()
+        self._check(self._lib.ast2o_set(self._h, name.encode(), a.ctypes.data, a.size))
+
+    def info(self):
+        """dict: substeps (last frame), unknowns, pcg_iters, pcg_ok, nnz, substeps_total."""
+        out = (ctypes.c_long * 6)()
+        self._lib.ast2o_info(self._h, out)
+        keys = ["substeps", "unknowns", "pcg_iters", "pcg_ok", "nnz", "substeps_total"]
+        return dict(zip(keys, list(out)))

@@ -27,6 +27,17 @@ the state it restores from them with OctreeOmniGridSolver3::restart in a fresh s
 projection, as in the step fixtures).
 
     python tests/golden/make_golden.py --ckpt-only
+
+2-D fixtures (ref2d_*.npz): the uniform 2-D solver ASTSolver<2> run by oracle/ref/ref_harness2d.cpp
+with Solver::update's CFL sub-stepping, in the reference's storage order (x fastest): init/<field>,
+the state after every frame f<k>/<field>, per-stage snapshots f<k>/s<j>/<stage>/<field> of the
+first frames (stages source, force, project, advect; project also holds A_rowptr, A_col, A_val,
+b, p), substeps (per frame) and sub_dt.  The "stock" cases run the reference as it is; the "eval"
+cases run ref_harness2d_eval, which evaluates the correction term of ASTFaceGrid<double, 2>::sample
+that the stock code reads from a destroyed temporary (see ref_harness2d.cpp).  Values of closed
+tilts are stale pool memory in the reference and are not meaningful.
+
+    python tests/golden/make_golden.py --2d-only
 """
 import os
 import subprocess
@@ -55,6 +66,29 @@ EXTRAP_CASES = [
     ("ref_extrap_c8_l3", 8, 3, 2, (0.47, 0.53, 0.29, 0.15, 4.0, 0.0)),
     ("ref_extrap_c16_l2", 16, 2, 2, (0.52, 0.44, 0.21, 0.11, 6.0, 0.5)),
 ]
+
+CASES2D = [
+    # name, harness, nx, ny, frames, dt, adaptive, frames with stage snapshots
+    ("ref2d_stock_n32", "ref_harness2d", 32, 64, 3, 0.02500000037252903, 0, 1),
+    ("ref2d_stock_a48", "ref_harness2d", 48, 96, 1, 0.02500000037252903, 1, 1),
+    ("ref2d_eval_a48", "ref_harness2d_eval", 48, 96, 4, 0.02500000037252903, 1, 2),
+    ("ref2d_eval_a32_substeps", "ref_harness2d_eval", 32, 64, 3, 0.3, 1, 0),
+]
+DROP2D = ("dual_vert",)
+
+
+def fixtures_2d():
+    for name, exe, nx, ny, frames, dt, adaptive, stage_frames in CASES2D:
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "out.astg")
+            subprocess.check_call([os.path.join(ROOT, "oracle", "_ref", exe), str(nx), str(ny), str(frames), repr(dt),
+                                   str(adaptive), path, str(stage_frames)], stdout=subprocess.DEVNULL)
+            out = {k: v for k, v in astg_archive.read(path).items() if not k.endswith(DROP2D)}
+            out["meta/case"] = np.array([nx, ny, frames, adaptive, stage_frames], dtype=np.int32)
+            out["meta/dt"] = np.array([dt], dtype=np.float64)
+            dst = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(dst, **out)
+            print(f"{dst}: {os.path.getsize(dst) / 1e6:.2f} MB, {len(out)} arrays")
 
 
 def extrap_fixtures(harness):
@@ -108,6 +142,9 @@ def main():
     subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref", "Makefile"), f"REF={ref}",
                            "-j8"])
     harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+    if "--2d-only" in sys.argv:
+        fixtures_2d()
+        return
     if "--ckpt-only" not in sys.argv:
         extrap_fixtures(harness)
     if "--extrap-only" in sys.argv:
