@@ -7,6 +7,8 @@ module on a machine without it raises instead of falling back to anything.
 """
 import ctypes
 import os
+import sys
+import time
 
 import numpy as np
 
@@ -24,7 +26,10 @@ SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_erro
            "astg_set_solver_parameters", "astg_set_precision", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
            "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate",
            "astg_restart", "astg_save_checkpoint", "astg_tape_start", "astg_tape_stop", "astg_adjoint_reset",
-           "astg_backward", "astg_step_vjp", "astg_stage_vjp", "astg_adjoint_probe", "astg_set_tilt_adaptivity"]
+           "astg_backward", "astg_step_vjp", "astg_stage_vjp", "astg_adjoint_probe", "astg_set_tilt_adaptivity",
+           # include/astg2d.h (uniform 2-D AST solver)
+           "astg2_create", "astg2_destroy", "astg2_last_error", "astg2_update", "astg2_stage", "astg2_get_density",
+           "astg2_count", "astg2_get", "astg2_set", "astg2_set_solver", "astg2_last_stats"]
 
 
 class AstgError(RuntimeError):
@@ -57,6 +62,12 @@ class SolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("outer", ctypes.c_int), ("converged", ctypes.c_int),
                 ("n", ctypes.c_int), ("nnz", ctypes.c_longlong), ("residual", ctypes.c_double),
                 ("tolerance", ctypes.c_double), ("ms", ctypes.c_double)]
+
+
+class Stats2D(ctypes.Structure):
+    _fields_ = [("substeps", ctypes.c_int), ("unknowns", ctypes.c_int), ("pcg_iterations", ctypes.c_int),
+                ("pcg_converged", ctypes.c_int), ("nnz", ctypes.c_longlong), ("pcg_residual", ctypes.c_double),
+                ("ms", ctypes.c_double), ("substeps_total", ctypes.c_longlong)]
 
 
 class StepStats(ctypes.Structure):
@@ -108,6 +119,21 @@ def lib(path=None):
         L.astg_step_vjp.argtypes = [c_p, ctypes.c_double]
         L.astg_stage_vjp.argtypes = [c_p, ctypes.c_int, ctypes.c_double]
         L.astg_adjoint_probe.argtypes = [c_p, ctypes.c_int, ctypes.c_int, c_p, c_p]
+        L.astg2_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(c_p)]
+        L.astg2_destroy.argtypes = [c_p]
+        L.astg2_last_error.argtypes = [c_p]
+        L.astg2_last_error.restype = ctypes.c_char_p
+        L.astg2_update.argtypes = [c_p, ctypes.c_double]
+        L.astg2_stage.argtypes = [c_p, ctypes.c_int, ctypes.c_double]
+        L.astg2_get_density.argtypes = [c_p, c_p, ctypes.c_longlong]
+        L.astg2_count.argtypes = [c_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+        L.astg2_count.restype = ctypes.c_longlong
+        L.astg2_get.argtypes = [c_p, ctypes.c_char_p, c_p, ctypes.c_longlong]
+        L.astg2_set.argtypes = [c_p, ctypes.c_char_p, c_p, ctypes.c_longlong]
+        L.astg2_set_solver.argtypes = [c_p, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_int]
+        L.astg2_last_stats.argtypes = [c_p, ctypes.POINTER(Stats2D)]
         _lib = L
     return _lib
 
@@ -426,3 +452,319 @@ def __getattr__(name):
         globals()[name] = fn
         return fn
     raise AttributeError(name)
+
+
+# ----------------------------------------------------------------------------------------------
+# The reference module's uniform-grid surface (python_bindings/ast_solver.cc:14-80)
+
+def _index(res, d, what):
+    t = tuple(int(v) for v in np.asarray(res).ravel())
+    if len(t) != d or min(t) < 1:
+        raise ValueError(f"{what}: resolution must hold {d} positive integers")
+    return t
+
+
+class ASTGrid2:
+    """ASTGrid<REAL, 2> (include/ast_grid.h:30); the module binds only dimension()."""
+
+    def dimension(self):
+        return 2
+
+
+class ASTGrid3:
+    """ASTGrid<REAL, 3>; the module binds only dimension()."""
+
+    def dimension(self):
+        return 3
+
+
+class TiltNode2:
+    """TiltNode<2> (include/ast_grid_layout.h:14-58): one tilted cell of a layout."""
+
+    def __init__(self, is_open=False):
+        self._open = bool(is_open)
+
+    def open(self):
+        return self._open
+
+
+class TiltNode3(TiltNode2):
+    """TiltNode<3>."""
+
+
+class CellNode2:
+    """CellNode<2> (include/ast_grid_layout.h:60-92); the module binds no members."""
+
+
+class CellNode3:
+    """CellNode<3>; the module binds no members."""
+
+
+class ASTGridLayout2:
+    """ASTGridLayout<2>(res, dx) (include/ast_grid_layout.h:134-140) with the bound read-only
+    properties ``resolution`` and ``dx``.  Every tilt of a new layout is closed."""
+
+    _d = 2
+
+    def __init__(self, res, dx):
+        self._res = _index(res, self._d, type(self).__name__)
+        self._dx = float(dx)
+
+    @property
+    def resolution(self):
+        return np.array(self._res, dtype=np.int32)
+
+    @property
+    def dx(self):
+        return self._dx
+
+
+class ASTGridLayout3(ASTGridLayout2):
+    """ASTGridLayout<3>(res, dx)."""
+
+    _d = 3
+
+
+class ASTSolver2:
+    """ASTSolver<2>(resolution, dx, adaptive_dofs, name) on the GPU (include/astg2d.h): the
+    reference's uniform 2-D AST smoke solver.  ``initialize()``, ``update(dt)`` (Solver::update's CFL
+    sub-stepping) and ``getDensity()`` (the cell densities, a copy) are the bound methods; the rest
+    (``get``, ``set``, ``stage``, ``last_stats``) read and drive the state for checks."""
+
+    FIELDS = {"density_cell", "heat_cell", "density_vert", "heat_vert", "mac_x", "mac_y", "tilt_vel", "dual_vert",
+              "tilt_open", "pindex_cell", "pindex_vert", "A_rowptr", "A_col", "A_val", "b", "p", "sub_dt"}
+    STAGES = {"source": 0, "force": 1, "project": 2, "advect": 3, "substep": 4}
+
+    def __init__(self, resolution, dx, adaptive_dofs=True, name="ASTSolver", device=0):
+        self.resolution = _index(resolution, 2, "ASTSolver2")
+        self.dx = float(dx)
+        self.adaptive_dofs = bool(adaptive_dofs)
+        self.name = name
+        self.device = device
+        self._h = None
+        self._lib = lib()
+
+    def initialize(self):
+        """ASTSolver::initialize (include/ast_solver.h:35-50): zero fields, boundary tilts fixed
+        closed, cells numbered."""
+        self.close()
+        h = ctypes.c_void_p()
+        nx, ny = self.resolution
+        st = self._lib.astg2_create(nx, ny, self.dx, 1 if self.adaptive_dofs else 0, self.device, ctypes.byref(h))
+        self._h = h
+        if st != ASTG_OK:
+            msg = self._lib.astg2_last_error(h).decode() if h.value else STATUS.get(st, "")
+            self.close()
+            raise AstgError(st, msg)
+
+    def close(self):
+        if self._h is not None and self._h.value:
+            self._lib.astg2_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _handle(self):
+        if self._h is None:  # Solver::update initialises on first use (src/solver.cpp:9-11)
+            self.initialize()
+        return self._h
+
+    def _check(self, st):
+        if st != ASTG_OK:
+            raise AstgError(st, self._lib.astg2_last_error(self._h).decode())
+
+    def update(self, dt):
+        h = self._handle()
+        _benchmark_timer.start_section("update")
+        try:
+            self._check(self._lib.astg2_update(h, float(dt)))
+        finally:
+            _benchmark_timer.stop_section("update")
+
+    def stage(self, name, dt):
+        self._check(self._lib.astg2_stage(self._handle(), self.STAGES[name], float(dt)))
+
+    def getDensity(self):
+        h = self._handle()
+        n = self.resolution[0] * self.resolution[1]
+        out = np.empty(n, dtype=np.float64)
+        self._check(self._lib.astg2_get_density(h, out.ctypes.data, n))
+        return out
+
+    def _shape(self, name, n):
+        nx, ny = self.resolution
+        shapes = {"density_cell": (ny, nx), "heat_cell": (ny, nx), "pindex_cell": (ny, nx),
+                  "density_vert": (ny + 1, nx + 1), "heat_vert": (ny + 1, nx + 1), "tilt_open": (ny + 1, nx + 1),
+                  "pindex_vert": (ny + 1, nx + 1), "mac_x": (ny, nx + 1), "mac_y": (ny + 1, nx),
+                  "tilt_vel": (ny + 1, nx + 1, 4), "dual_vert": (ny + 1, nx + 1, 2)}
+        return shapes.get(name, (n,))
+
+    def get(self, name):
+        h = self._handle()
+        kind = ctypes.c_int(0)
+        n = self._lib.astg2_count(h, name.encode(), ctypes.byref(kind))
+        if n < 0:
+            raise KeyError(name)
+        out = np.empty(n, dtype=[np.float64, np.uint8, np.int32][kind.value])
+        self._check(self._lib.astg2_get(h, name.encode(), out.ctypes.data, n))
+        return out.reshape(self._shape(name, n))
+
+    def set(self, name, arr):
+        h = self._handle()
+        a = np.ascontiguousarray(arr, dtype=np.uint8 if name == "tilt_open" else np.float64).ravel()
+        self._check(self._lib.astg2_set(h, name.encode(), a.ctypes.data, a.size))
+
+    def set_solver_parameters(self, tol=1e-5, max_iter=5000, omega=0.97, min_diag=0.95, precision=FP64):
+        self._check(self._lib.astg2_set_solver(self._handle(), tol, max_iter, omega, min_diag, precision))
+
+    def last_stats(self):
+        s = Stats2D()
+        self._lib.astg2_last_stats(self._handle(), ctypes.byref(s))
+        return {k: getattr(s, k) for k, _ in Stats2D._fields_}
+
+
+class ASTSolver3:
+    """ASTSolver<3>(resolution, dx, adaptive_dofs, name).  The reference's uniform 3-D AST path is
+    unfinished (its 3-D scene and edge nodes are TODO, include/ast_solver.h:97-100, 207) and its
+    update aborts on an Eigen bounds assertion in the second step once tilts open, so it is not
+    built here: construction keeps the arguments, initialize() and update() raise.  The octree
+    smoke solver (``OctreeSmoke3``) is the 3-D path."""
+
+    def __init__(self, resolution, dx, adaptive_dofs=True, name="ASTSolver"):
+        self.resolution = _index(resolution, 3, "ASTSolver3")
+        self.dx = float(dx)
+        self.adaptive_dofs = bool(adaptive_dofs)
+        self.name = name
+
+    def _refuse(self, *a):
+        raise NotImplementedError("ASTSolver3: the reference's uniform 3-D AST solver is incomplete (its update "
+                                  "aborts once tilts open); use OctreeSmoke3")
+
+    initialize = update = getDensity = _refuse
+
+
+class _BenchmarkTimer:
+    """BenchmarkTimer (include/timer.h:67-235): named sections (nested as outer:inner) and timers
+    within the innermost open section, each with its elapsed seconds and invocation count."""
+
+    class _T:
+        def __init__(self):
+            self.running, self.time, self.invocations, self.t0 = False, 0.0, 0, 0.0
+            self.start()
+
+        def elapsed(self):
+            return self.time + (time.perf_counter() - self.t0 if self.running else 0.0)
+
+        def start(self):
+            if self.running:
+                print("ERROR: timer already running. Reported timings will be inaccurate.", file=sys.stderr)
+                self.stop()
+            self.running, self.t0 = True, time.perf_counter()
+            self.invocations += 1
+
+        def stop(self):
+            if self.running:
+                self.time += time.perf_counter() - self.t0
+                self.running = False
+
+    def __init__(self):
+        self.reset()
+
+    def reset(self):
+        self.sections = {"": (self._T(), {})}
+        self.stack = []
+
+    @staticmethod
+    def _display(name):
+        levels = name.count(":")
+        return name if levels == 0 else " " * (4 * levels) + name[name.rfind(":") + 1:]
+
+    def start_section(self, name):
+        if self.stack:
+            name = self.stack[-1] + ":" + name
+        self.stack.append(name)
+        if name in self.sections:
+            self.sections[name][0].start()
+        else:
+            self.sections[name] = (self._T(), {})
+
+    def stop_section(self, name):
+        if not self.stack:
+            raise RuntimeError("benchmark_stop_timer_section: no open section")
+        current = self.stack.pop()
+        if self.stack:
+            name = self.stack[-1] + ":" + name
+        if name != current:
+            print(f"ERROR: sections must be stopped in the reverse of the order they were started.\n"
+                  f"(Expected {current}, but got {name})", file=sys.stderr)
+        t, timers = self.sections[name]
+        t.stop()
+        for k, v in timers.items():
+            if v.running:
+                print(f"WARNING: stopping timer {k} implicitly in enclosing section's stop()", file=sys.stderr)
+                v.stop()
+
+    def _timer_name(self, name):
+        section = self.stack[-1] if self.stack else ""
+        return section, (section + ":" + name if section else name)
+
+    def start_timer(self, name):
+        section, full = self._timer_name(name)
+        timers = self.sections[section][1]
+        if full in timers:
+            timers[full].start()
+        else:
+            timers[full] = self._T()
+
+    def stop_timer(self, name):
+        section, full = self._timer_name(name)
+        self.sections[section][1][full].stop()
+
+    def report(self, out=None):
+        out = out or sys.stdout
+        for name in sorted(self.sections):
+            if name == "":
+                continue
+            t, timers = self.sections[name]
+            print(f"{self._display(name)}\t{t.elapsed()}\t{t.invocations}", file=out)
+            for k in sorted(timers):
+                print(f"{self._display(k)}\t{timers[k].elapsed()}\t{timers[k].invocations}", file=out)
+        t, timers = self.sections[""]
+        for k in sorted(timers):
+            print(f"{self._display(k)}\t{timers[k].elapsed()}\t{timers[k].invocations}", file=out)
+        print(f"Full time\t{t.elapsed()}", file=out)
+
+
+_benchmark_timer = _BenchmarkTimer()
+_benchmark_messages = []
+
+
+def benchmark_reset():
+    _benchmark_timer.reset()
+
+
+def benchmark_start_timer_section(name):
+    _benchmark_timer.start_section(name)
+
+
+def benchmark_stop_timer_section(name):
+    _benchmark_timer.stop_section(name)
+
+
+def benchmark_start_timer(name):
+    _benchmark_timer.start_timer(name)
+
+
+def benchmark_stop_timer(name):
+    _benchmark_timer.stop_timer(name)
+
+
+def benchmark_report(include_messages=False):
+    if include_messages:
+        for m in _benchmark_messages:
+            print(m)
+    _benchmark_timer.report()

@@ -609,110 +609,11 @@ struct astg_handle {
     void allocProj() {
         long long rows = rowCapacity();
         if (rows * ROW_W >= (1LL << 31)) throw std::invalid_argument("octree too large for 32-bit matrix indices");
-        J.rowsCap = (int)rows;
         J.cnt = dalloc<int>(S);
         J.base = dalloc<int>(S);
-        J.n0 = dalloc<int>(1);
-        J.nDof = dalloc<int>(1);
-        J.nnz = dalloc<int>(4);  // nnz, then scan totals of the level schedule
         J.pO = dalloc<int>(S);
         J.pT = dalloc<int>(S);
-        J.rowCnt = dalloc<int>(rows);
-        J.rowPtr = dalloc<int>(rows + 1);
-        J.padCol = dalloc<int>(rows * ROW_W);
-        J.padVal = dalloc<double>(rows * ROW_W);
-        J.bRaw = dalloc<double>(rows);
-        J.col = dalloc<int>(rows * ROW_W);
-        J.val = dalloc<double>(rows * ROW_W);
-        J.diagPos = dalloc<int>(rows);
-        J.tpos = dalloc<int>(rows * ROW_W);
-        J.b = dalloc<double>(rows);
-        J.Lv = dalloc<double>(rows * ROW_W);
-        J.invdiag = dalloc<double>(rows);
-        J.adiag = dalloc<double>(rows);
-        J.ready = dalloc<int>(rows);
-        J.planPtr = dalloc<int>(rows * ROW_W + 1);
-        J.planCap = rows * ROW_W * 2;
-        J.plan = dalloc<int>(J.planCap);
-        J.planTotal = dalloc<int>(1);
-        J.counter = dalloc<int>(1);
-        J.level = dalloc<int>(rows);
-        J.levelCnt = dalloc<int>(rows + 1);
-        J.levelPtr = dalloc<int>(rows + 2);
-        J.nLevels = dalloc<int>(1);
-        J.fill = dalloc<int>(rows + 1);
-        J.perm = dalloc<int>(rows);
-        J.cntF = dalloc<int>(rows);
-        J.cntB = dalloc<int>(rows);
-        J.fptr = dalloc<int>(rows + 1);
-        J.bptr = dalloc<int>(rows + 1);
-        J.fcol = dalloc<int>(rows * ROW_W / 2 + 1);
-        J.fval = dalloc<double>(rows * ROW_W / 2 + 1);
-        J.bcol = dalloc<int>(rows * ROW_W / 2 + 1);
-        J.bval = dalloc<double>(rows * ROW_W / 2 + 1);
-        // MIC(0) sweep form: ASTG_SWEEP = async (default: fused, barrier-free), dsmem (fused, one
-        // cluster barrier per level), cluster (global-memory level sweeps) or syncfree (per-row
-        // flags); a form the device cannot run falls back to the next one
-        const char* env = getenv("ASTG_SWEEP");
-        std::string mode = env ? env : "async";
-        if (mode != "async" && mode != "dsmem" && mode != "cluster" && mode != "syncfree")
-            throw std::invalid_argument("ASTG_SWEEP must be async, dsmem, cluster or syncfree");
-        J.clusterSize = mode == "syncfree" ? 0 : choose_cluster_size(P.device);
-        J.pcAsync = mode == "async";
-        J.pcCluster = (mode == "async" || mode == "dsmem") ? choose_dsmem_cluster(J.pcAsync, &J.pcSmemMax) : 0;
-        J.pcActive = 0;
-        J.pcSmem = 0;
-        J.pcLgBlock = 8;  // 256-row ownership blocks (measured: 64 to 4096 within 3 %)
-        long long scanMax = std::max(rows * ROW_W + 1, (long long)std::max(J.pcCluster, 1) * (rows + 1));
-        J.bsum = dalloc<int>((scanMax + 1023) / 1024 + 1);
-        if (J.pcCluster && J.pcAsync) {
-            J.chunk = dalloc<int>(1);
-            J.ownStart = dalloc<int>(J.pcCluster + 1);
-            // FP32 copies for the mixed-precision solve
-            J.val32 = dalloc<float>(rows * ROW_W);
-            J.fvalP32 = dalloc<float>(rows * PC_MAXE);
-            J.bvalP32 = dalloc<float>(rows * PC_MAXE);
-            J.linvd32 = dalloc<float>(rows);
-            J.rl32 = dalloc<float>(rows);
-            J.yl32 = dalloc<float>(rows);
-            J.fval32 = dalloc<float>(rows * ROW_W / 2 + 1);
-            J.bval32 = dalloc<float>(rows * ROW_W / 2 + 1);
-            J.e32 = dalloc<float>(rows);
-            J.r32 = dalloc<float>(rows);
-            J.s32 = dalloc<float>(rows);
-            J.z32 = dalloc<float>(rows);
-            J.q32 = dalloc<float>(rows);
-            J.lself = dalloc<int>(rows);
-            J.yl = dalloc<double>(rows);
-            J.ownCnt = dalloc<int>((rows + 1) * J.pcCluster);
-            J.ownPtr = dalloc<int>((rows + 1) * J.pcCluster + 1);
-            J.ownFill = dalloc<int>((rows + 1) * J.pcCluster);
-        }
-        if (J.pcCluster) {
-            J.pos = dalloc<int>(rows);
-            J.lcntF = dalloc<int>(rows);
-            J.lcntB = dalloc<int>(rows);
-            J.linvd = dalloc<double>(rows);
-            J.rl = dalloc<double>(rows);
-            J.fcolP = dalloc<int>(rows * PC_MAXE);
-            J.fvalP = dalloc<double>(rows * PC_MAXE);
-            J.bcolP = dalloc<int>(rows * PC_MAXE);
-            J.bvalP = dalloc<double>(rows * PC_MAXE);
-        }
-        int sms = 0;
-        ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P.device), "attr");
-        J.sweepBlocks = std::max(1, sms) * 8;
-        J.x = dalloc<double>(rows);
-        J.r = dalloc<double>(rows);
-        J.s = dalloc<double>(rows);
-        J.z = dalloc<double>(rows);
-        J.part = dalloc<double>((rows + 2047) / 2048 + 1);
-        J.sc = dalloc<double>(SC_COUNT);
-        J.isc = dalloc<int>(ISC_COUNT);
-        J.amax = dalloc<unsigned long long>(1);
-        J.done = dalloc<int>(1);
-        ck(cudaMallocHost(&J.hostDone, sizeof(int)), "cudaMallocHost");
-        *J.hostDone = 0;
+        proj_alloc(J, rows, P.device, st, allocs);
     }
 
     // ---------------------------------------------------------------- step

@@ -1,6 +1,7 @@
 // Host-side declarations of the kernel launchers (implemented in astg_step.cu and astg_pcg.cu).
 #pragma once
 #include <cuda_runtime.h>
+#include <vector>
 #include "astg_device.cuh"
 
 namespace astg {
@@ -147,6 +148,8 @@ struct Proj {
     unsigned long long* amax;
     int* done;
     int* hostDone;   // pinned host
+    int tolAbsolute; // 1: the PCG stops at |r|_inf <= tol (the std::vector PCGSolver::solve overload,
+                     // include/pcgsolver/pcg_solver.h:302-363); 0: at tol * |b|_inf
 };
 
 void launch_source(const Dev& d, const Fields& F, cudaStream_t st);
@@ -174,6 +177,15 @@ void launch_assemble(const Dev& d, const Fields& F, const uint8_t* open, Proj& P
 // owner: the owner-major walk of the barrier-free preconditioner, else the level order
 void launch_level_schedule(const Dev& d, Proj& P, bool owner, cudaStream_t st);
 void launch_external_system(const Dev& d, Proj& P, int rows, cudaStream_t st);
+// padded rows (rowCnt, padCol, padVal, bRaw over maxRows rows, *nDof set) -> CSR with b = bRaw *
+// scale, diagonal positions and mirrored-entry positions
+void launch_rows_to_csr(const Dev& d, Proj& P, int maxRows, double scale, cudaStream_t st);
+// out = exclusive scan of in[0..n), *total = its sum; bsum holds ceil(n / 1024) + 1 ints
+void launch_exclusive_scan(const int* in, int* out, int* bsum, int* total, long long n, cudaStream_t st);
+// the row-sized projection workspace (everything but the per-slot numbering arrays cnt, base, pO,
+// pT) for `rows` rows on `device`, zeroed on `st`; each allocation is appended to `allocs`, which the
+// caller frees with cudaFree (and J.hostDone with cudaFreeHost).  Throws std::runtime_error.
+void proj_alloc(Proj& J, long long rows, int device, cudaStream_t st, std::vector<void*>& allocs);
 int choose_cluster_size(int device);
 // cluster size (16 or 8) for the fused preconditioner (barrier-free form when async), or 0
 int choose_dsmem_cluster(bool async, size_t* smemMax);

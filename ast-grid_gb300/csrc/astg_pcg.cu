@@ -22,6 +22,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
 
 #include "astg_launch.h"
 #include "astg_sample.cuh"
@@ -679,10 +682,16 @@ void launch_assemble(const Dev& d, const Fields& F, const uint8_t* open, Proj& P
     ASTG_LAUNCH(k_asm_oct<<<nblk(d.S), TB, 0, st>>>(d, F, P, hoPtr, hoIdx));
     ASTG_LAUNCH(k_asm_tilt<<<nblk(d.S), TB, 0, st>>>(d, F, P, open));
     if (d.H) ASTG_LAUNCH(k_asm_half<<<nblk(d.H), TB, 0, st>>>(d, F, P));
+    launch_rows_to_csr(d, P, maxRows, d.rho / dt, st);
+}
+void launch_rows_to_csr(const Dev& d, Proj& P, int maxRows, double scale, cudaStream_t st) {
     exclusive_scan(P.rowCnt, P.rowPtr, P.bsum, P.nnz, maxRows, st);
     ASTG_LAUNCH(k_rowptr_last<<<1, 1, 0, st>>>(P));
-    ASTG_LAUNCH(k_csr_fill<<<nblk(maxRows), TB, 0, st>>>(P, d.rho / dt));
+    ASTG_LAUNCH(k_csr_fill<<<nblk(maxRows), TB, 0, st>>>(P, scale));
     ASTG_LAUNCH(k_transpose_map<<<nblk(maxRows), TB, 0, st>>>(d, P));
+}
+void launch_exclusive_scan(const int* in, int* out, int* bsum, int* total, long long n, cudaStream_t st) {
+    exclusive_scan(in, out, bsum, total, n, st);
 }
 
 // ------------------------------------------------------------------ sync-free helpers
@@ -1573,7 +1582,7 @@ __global__ void k_pcg_start(Proj P, const double* partRho, double tolFactor) {
     if (threadIdx.x == 0) {
         double r0 = __longlong_as_double((long long)*P.amax);
         P.sc[SC_RESID0] = r0;
-        P.sc[SC_TOL] = tolFactor * r0;
+        P.sc[SC_TOL] = P.tolAbsolute ? tolFactor : tolFactor * r0;
         P.sc[SC_RHO] = rho;
         P.sc[SC_RESID] = r0;
         if (r0 == 0) { *P.done = 1; P.isc[ISC_ITERS] = 0; P.isc[ISC_CONVERGED] = 1; }
@@ -2084,7 +2093,7 @@ int launch_pcg_mixed(const Dev& d, Proj& P, double tolFactor, int maxIter, int b
     cudaMemsetAsync(P.isc, 0, sizeof(int) * ISC_COUNT, st);
     ASTG_LAUNCH(k_absmax<<<nblk(maxRows), TB, 0, st>>>(r, P.nDof, P.amax));
     const double res0 = read_amax(P, st);
-    const double tolAbs = tolFactor * res0;
+    const double tolAbs = P.tolAbsolute ? tolFactor : tolFactor * res0;
     double res = res0;
     int outer = 0, converged = 0;
     PcaData<float> D = pca_data32(P);
@@ -2145,4 +2154,129 @@ int launch_pcg_mixed(const Dev& d, Proj& P, double tolFactor, int maxIter, int b
     ASTG_LAUNCH(k_mixed_finish<<<1, 1, 0, st>>>(P, res, tolAbs, res0, converged));
     return outer;
 }
+// ------------------------------------------------------------------ workspace
+namespace {
+struct ProjArena {
+    cudaStream_t st;
+    std::vector<void*>& allocs;
+    void ck(cudaError_t e, const char* what) {
+        if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+    }
+    template <class T>
+    T* get(long long n) {
+        void* p = nullptr;
+        size_t bytes = (size_t)std::max<long long>(n, 1) * sizeof(T);
+        ck(cudaMalloc(&p, bytes), "cudaMalloc");
+        allocs.push_back(p);
+        ck(cudaMemsetAsync(p, 0, bytes, st), "cudaMemset");
+        return (T*)p;
+    }
+};
+}  // namespace
+
+void proj_alloc(Proj& J, long long rows, int device, cudaStream_t st, std::vector<void*>& allocs) {
+    if (rows <= 0 || rows * ROW_W >= (1LL << 31)) throw std::runtime_error("projection too large for 32-bit matrix indices");
+    ProjArena A{st, allocs};
+    J.rowsCap = (int)rows;
+    J.n0 = A.get<int>(1);
+    J.nDof = A.get<int>(1);
+    J.nnz = A.get<int>(4);  // nnz, then scan totals of the level schedule
+    J.rowCnt = A.get<int>(rows);
+    J.rowPtr = A.get<int>(rows + 1);
+    J.padCol = A.get<int>(rows * ROW_W);
+    J.padVal = A.get<double>(rows * ROW_W);
+    J.bRaw = A.get<double>(rows);
+    J.col = A.get<int>(rows * ROW_W);
+    J.val = A.get<double>(rows * ROW_W);
+    J.diagPos = A.get<int>(rows);
+    J.tpos = A.get<int>(rows * ROW_W);
+    J.b = A.get<double>(rows);
+    J.Lv = A.get<double>(rows * ROW_W);
+    J.invdiag = A.get<double>(rows);
+    J.adiag = A.get<double>(rows);
+    J.ready = A.get<int>(rows);
+    J.planPtr = A.get<int>(rows * ROW_W + 1);
+    J.planCap = rows * ROW_W * 2;
+    J.plan = A.get<int>(J.planCap);
+    J.planTotal = A.get<int>(1);
+    J.counter = A.get<int>(1);
+    J.level = A.get<int>(rows);
+    J.levelCnt = A.get<int>(rows + 1);
+    J.levelPtr = A.get<int>(rows + 2);
+    J.nLevels = A.get<int>(1);
+    J.fill = A.get<int>(rows + 1);
+    J.perm = A.get<int>(rows);
+    J.cntF = A.get<int>(rows);
+    J.cntB = A.get<int>(rows);
+    J.fptr = A.get<int>(rows + 1);
+    J.bptr = A.get<int>(rows + 1);
+    J.fcol = A.get<int>(rows * ROW_W / 2 + 1);
+    J.fval = A.get<double>(rows * ROW_W / 2 + 1);
+    J.bcol = A.get<int>(rows * ROW_W / 2 + 1);
+    J.bval = A.get<double>(rows * ROW_W / 2 + 1);
+    // MIC(0) sweep form: ASTG_SWEEP = async (default: fused, barrier-free), dsmem (fused, one
+    // cluster barrier per level), cluster (global-memory level sweeps) or syncfree (per-row
+    // flags); a form the device cannot run falls back to the next one
+    const char* env = getenv("ASTG_SWEEP");
+    std::string mode = env ? env : "async";
+    if (mode != "async" && mode != "dsmem" && mode != "cluster" && mode != "syncfree")
+        throw std::invalid_argument("ASTG_SWEEP must be async, dsmem, cluster or syncfree");
+    J.clusterSize = mode == "syncfree" ? 0 : choose_cluster_size(device);
+    J.pcAsync = mode == "async";
+    J.pcCluster = (mode == "async" || mode == "dsmem") ? choose_dsmem_cluster(J.pcAsync, &J.pcSmemMax) : 0;
+    J.pcActive = 0;
+    J.pcSmem = 0;
+    J.pcLgBlock = 8;  // 256-row ownership blocks (measured: 64 to 4096 within 3 %)
+    long long scanMax = std::max(rows * ROW_W + 1, (long long)std::max(J.pcCluster, 1) * (rows + 1));
+    J.bsum = A.get<int>((scanMax + 1023) / 1024 + 1);
+    if (J.pcCluster && J.pcAsync) {
+        J.chunk = A.get<int>(1);
+        J.ownStart = A.get<int>(J.pcCluster + 1);
+        // FP32 copies for the mixed-precision solve
+        J.val32 = A.get<float>(rows * ROW_W);
+        J.fvalP32 = A.get<float>(rows * PC_MAXE);
+        J.bvalP32 = A.get<float>(rows * PC_MAXE);
+        J.linvd32 = A.get<float>(rows);
+        J.rl32 = A.get<float>(rows);
+        J.yl32 = A.get<float>(rows);
+        J.fval32 = A.get<float>(rows * ROW_W / 2 + 1);
+        J.bval32 = A.get<float>(rows * ROW_W / 2 + 1);
+        J.e32 = A.get<float>(rows);
+        J.r32 = A.get<float>(rows);
+        J.s32 = A.get<float>(rows);
+        J.z32 = A.get<float>(rows);
+        J.q32 = A.get<float>(rows);
+        J.lself = A.get<int>(rows);
+        J.yl = A.get<double>(rows);
+        J.ownCnt = A.get<int>((rows + 1) * J.pcCluster);
+        J.ownPtr = A.get<int>((rows + 1) * J.pcCluster + 1);
+        J.ownFill = A.get<int>((rows + 1) * J.pcCluster);
+    }
+    if (J.pcCluster) {
+        J.pos = A.get<int>(rows);
+        J.lcntF = A.get<int>(rows);
+        J.lcntB = A.get<int>(rows);
+        J.linvd = A.get<double>(rows);
+        J.rl = A.get<double>(rows);
+        J.fcolP = A.get<int>(rows * PC_MAXE);
+        J.fvalP = A.get<double>(rows * PC_MAXE);
+        J.bcolP = A.get<int>(rows * PC_MAXE);
+        J.bvalP = A.get<double>(rows * PC_MAXE);
+    }
+    int sms = 0;
+    A.ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attr");
+    J.sweepBlocks = std::max(1, sms) * 8;
+    J.x = A.get<double>(rows);
+    J.r = A.get<double>(rows);
+    J.s = A.get<double>(rows);
+    J.z = A.get<double>(rows);
+    J.part = A.get<double>((rows + 2047) / 2048 + 1);
+    J.sc = A.get<double>(SC_COUNT);
+    J.isc = A.get<int>(ISC_COUNT);
+    J.amax = A.get<unsigned long long>(1);
+    J.done = A.get<int>(1);
+    A.ck(cudaMallocHost(&J.hostDone, sizeof(int)), "cudaMallocHost");
+    *J.hostDone = 0;
+}
+
 }  // namespace astg

@@ -1,5 +1,5 @@
 """CPU checks of the drop-in boundary: the CUDA library builds, loads and exports every entry
-point include/astg.h declares; the Python front end refuses to run without it."""
+point include/astg.h and include/astg2d.h declare; the Python front end refuses to run without it."""
 import os
 import re
 import sys
@@ -13,9 +13,12 @@ if PKG not in sys.path:
 
 
 def declared_symbols():
-    txt = open(os.path.join(ROOT, "include", "astg.h")).read()
-    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(astg_[a-z_0-9]+)\s*\(", txt)))
+    out = set()
+    for h in ("astg.h", "astg2d.h"):
+        txt = open(os.path.join(ROOT, "include", h)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        out |= set(re.findall(r"\b(astg2?_[a-z_0-9]+)\s*\(", txt))
+    return sorted(out)
 
 
 def test_library_exports_every_declared_symbol():
