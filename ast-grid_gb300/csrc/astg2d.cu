@@ -435,6 +435,225 @@ __global__ void k2_cfl(Grid2 g, const double* mx, const double* my, unsigned lon
     if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
 }
 
+
+// ------------------------------------------------------------------ wavefront MIC(0) sweeps
+// The system's cells come first in raster order, so a cell's lower neighbours are the cells below
+// and to the left (one anti-diagonal earlier) and its upper ones the cells to the right and above
+// and its open corner tilts; a tilt row's lower neighbours are its four cells and it has no upper
+// ones.  The forward sweep is therefore one anti-diagonal per step (the cells of a diagonal are
+// independent), then the tilt rows in one pass; the backward sweep the tilt rows, then the
+// diagonals in reverse.  Every row applies its updates in ascending column order with one fused
+// multiply-subtract each and multiplies by its pivot reciprocal last -- the generic sweeps'
+// arithmetic (and the oracle's in reduce mode 1), so the result is bit-identical.
+//
+// One CTA, one thread per column (column x = lane x % 32 of warp x / 32), one block barrier per
+// diagonal.  A column's own previous result is the neighbour below (forward) or above (backward)
+// and stays in a register; the neighbour to the left / right is the adjacent lane's previous
+// result (a warp shuffle), across a warp boundary a shared-memory slot per warp and step parity.
+// The per-cell records, the residual and the results are stored diagonal-major (cell (x, y) at
+// x + (x + y) * nx), so every step's accesses are contiguous across a warp; they are loaded WAVE_PF
+// steps ahead.  A second kernel returns the cells' result to the system's order.  (A barrier-free form with per-warp progress counters measured 1.5x slower: its per-step
+// handshake and fences cost more than the barrier.)
+constexpr int WAVE_PF = 4;
+constexpr int WAVE_MAX_NX = 512;
+constexpr int WAVE_MAX_W = WAVE_MAX_NX / 32;
+
+// records of the factorised system for the wavefront kernel (one thread per row)
+__global__ void k2_wave_gather(Proj P, const int* vIdx) {
+    const int nx = P.wnx, ny = P.wny, nc = nx * ny;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= *P.nDof) return;
+    const int q0 = P.rowPtr[r], q1 = P.rowPtr[r + 1];
+    if (r >= nc) {  // tilt row: its cells (all columns below r), ascending
+        const int t = r - nc;
+        int k = 0;
+        for (int q = q0; q < q1 && k < 4; ++q) {
+            int col = P.col[q];
+            if (col >= r) break;
+            P.wTc[4 * t + k] = col;
+            P.wTv[4 * t + k] = P.Lv[P.tpos[q]];
+            ++k;
+        }
+        for (; k < 4; ++k) {  // an interior tilt always has four cells
+            P.wTc[4 * t + k] = -1;
+            P.wTv[4 * t + k] = 0;
+        }
+        return;
+    }
+    const int x = r % nx, y = r / nx, j = x + (x + y) * nx;  // diagonal-major slot
+    const int corner[4] = {vIdx[x + y * (nx + 1)], vIdx[x + 1 + y * (nx + 1)], vIdx[x + (y + 1) * (nx + 1)],
+                           vIdx[x + 1 + (y + 1) * (nx + 1)]};
+    double lb = 0, ll = 0, lr = 0, la = 0;
+    unsigned f = 0;
+    for (int k = 0; k < 4; ++k) {
+        P.wTt[4 * j + k] = -1;
+        P.wTl[4 * j + k] = 0;
+    }
+    for (int q = q0; q < q1; ++q) {
+        const int col = P.col[q];
+        if (col == r - nx) { lb = P.Lv[P.tpos[q]]; f |= 1; }
+        else if (col == r - 1) { ll = P.Lv[P.tpos[q]]; f |= 2; }
+        else if (col == r + 1) { lr = P.Lv[q]; f |= 4; }
+        else if (col == r + nx) { la = P.Lv[q]; f |= 8; }
+        else if (col >= nc) {
+            for (int k = 0; k < 4; ++k)
+                if (corner[k] == col) {
+                    P.wTt[4 * j + k] = col;
+                    P.wTl[4 * j + k] = P.Lv[q];
+                    f |= 16u << k;
+                }
+        }
+    }
+    const double inv = P.invdiag[r], fb = __longlong_as_double((long long)f);
+    P.wRecF[2 * j] = make_double2(lb, ll);
+    P.wRecF[2 * j + 1] = make_double2(inv, fb);
+    P.wRecB[2 * j] = make_double2(lr, la);
+    P.wRecB[2 * j + 1] = make_double2(inv, fb);
+}
+
+constexpr unsigned WAVE_NONE = 0x80000000u;  // no cell in this column on this diagonal
+struct WStep {
+    double v, l0, l1, inv;
+    unsigned f;
+};
+// one slot's record; WAVE_NONE when the column has no cell on the diagonal (then nothing is
+// computed: a warp with no cell on a diagonal issues no FP64 work there)
+__device__ __forceinline__ void wload(const double2* rec, const double* val, int j, bool on, WStep& s) {
+    if (!on) {
+        s.f = WAVE_NONE;
+        return;
+    }
+    const double2 a = rec[2 * j], b = rec[2 * j + 1];
+    s.v = val[j];
+    s.l0 = a.x;
+    s.l1 = a.y;
+    s.inv = b.x;
+    s.f = (unsigned)__double_as_longlong(b.y);
+}
+
+// the cells' result from diagonal-major order to the system's
+__global__ void k2_wave_unskew(Proj P, double* z) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nx = P.wnx;
+    if (*P.done || i >= nx * P.wny) return;
+    const int x = i % nx;
+    z[i] = P.wZ[x + (x + i / nx) * nx];
+}
+
+__global__ void __launch_bounds__(WAVE_MAX_NX) k2_precond_wave(Proj P, const double* r, double* z) {
+    __shared__ double edge[2][WAVE_MAX_W];  // per step parity: each warp's boundary value
+    if (*P.done) return;
+    const int nx = P.wnx, ny = P.wny, nc = nx * ny, n = *P.nDof;
+    const int D = nx + ny - 1;
+    const int x = threadIdx.x, lane = x & 31, w = x >> 5, W = blockDim.x >> 5;
+    const bool mine = x < nx;  // lanes past the last column only take part in the exchanges
+    const unsigned FULL = 0xffffffffu;
+    WStep A[WAVE_PF], B[WAVE_PF];
+
+    // ---- forward over the cells: step d visits slot x + d * nx, the cell (x, d - x).  The update
+    // from the cell below (this column's previous result) is applied before the barrier that ends
+    // the previous step; the one from the left needs the neighbouring column's previous result
+    // (shuffle, or the boundary slot of the warp to the left for lane 0).
+    double zb = 0;  // this column's last result
+    double t = 0;   // the current slot's accumulator after the update from below
+    auto fload = [&](WStep* S, int d0) {
+#pragma unroll
+        for (int s = 0; s < WAVE_PF; ++s) {
+            const int d = d0 + s, y = d - x;
+            wload(P.wRecF, P.wR, x + d * nx, mine && y >= 0 && y < ny, S[s]);
+        }
+    };
+    auto below = [&](const WStep& c) {  // (x, y - 1)
+        return (!(c.f & WAVE_NONE) && (c.f & 1)) ? fma(-c.l0, zb, c.v) : c.v;
+    };
+    auto fstep = [&](const WStep& c, const WStep& nxt, int d) {
+        const int cur = d & 1, prv = cur ^ 1;
+        double zl = __shfl_up_sync(FULL, zb, 1);
+        const double ze = edge[prv][w > 0 ? w - 1 : 0];
+        if (lane == 0) zl = ze;
+        if (!(c.f & WAVE_NONE)) {
+            double acc = (c.f & 2) ? fma(-c.l1, zl, t) : t;  // (x - 1, y)
+            acc = acc * c.inv;
+            P.wZ[x + d * nx] = acc;
+            zb = acc;
+        }
+        if (lane == 31) edge[cur][w] = zb;
+        t = below(nxt);
+        __syncthreads();
+    };
+    fload(A, 0);
+    t = below(A[0]);
+    for (int g = 0; g < D; g += 2 * WAVE_PF) {
+        fload(B, g + WAVE_PF);
+#pragma unroll
+        for (int s = 0; s < WAVE_PF; ++s)
+            if (g + s < D) fstep(A[s], s + 1 < WAVE_PF ? A[s + 1] : B[0], g + s);
+        fload(A, g + 2 * WAVE_PF);
+#pragma unroll
+        for (int s = 0; s < WAVE_PF; ++s)
+            if (g + WAVE_PF + s < D) fstep(B[s], s + 1 < WAVE_PF ? B[s + 1] : A[0], g + WAVE_PF + s);
+    }
+
+    // ---- tilt rows: forward (their four cells), then their backward step (no upper entries)
+    for (int tr = nc + x; tr < n; tr += blockDim.x) {
+        const int i = tr - nc;
+        double acc = r[tr];
+        for (int k = 0; k < 4; ++k) {
+            const int c = P.wTc[4 * i + k];
+            if (c >= 0) acc = fma(-P.wTv[4 * i + k], P.wZ[c % nx + (c % nx + c / nx) * nx], acc);
+        }
+        const double inv = P.invdiag[tr];
+        acc = acc * inv;
+        z[tr] = acc * inv;
+    }
+    __syncthreads();
+
+    // ---- backward over the cells: step s visits diagonal D - 1 - s; the update from the right
+    // (neighbouring column, shuffle or boundary slot) comes first, then the one from above (this
+    // column's previous result), then the corner tilts
+    double za = 0;
+    auto bload = [&](WStep* S, int s0) {
+#pragma unroll
+        for (int s = 0; s < WAVE_PF; ++s) {
+            const int d = D - 1 - (s0 + s), y = d - x;
+            wload(P.wRecB, P.wZ, x + d * nx, mine && y >= 0 && y < ny, S[s]);
+        }
+    };
+    auto bstep = [&](const WStep& c, int st) {
+        const int cur = st & 1, prv = cur ^ 1;
+        double zr = __shfl_down_sync(FULL, za, 1);
+        const double ze = edge[prv][w + 1 < W ? w + 1 : w];
+        if (lane == 31) zr = ze;
+        if (!(c.f & WAVE_NONE)) {
+            double acc = c.v;
+            if (c.f & 4) acc = fma(-c.l0, zr, acc);  // (x + 1, y)
+            if (c.f & 8) acc = fma(-c.l1, za, acc);  // (x, y + 1)
+            const int j = x + (D - 1 - st) * nx;
+            if (c.f & 0xf0u) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (c.f & (16u << k)) acc = fma(-P.wTl[4 * j + k], z[P.wTt[4 * j + k]], acc);
+            }
+            acc = acc * c.inv;
+            P.wZ[j] = acc;  // in place: this slot's forward value was loaded steps ago
+            za = acc;
+        }
+        if (lane == 0) edge[cur][w] = za;
+        __syncthreads();
+    };
+    bload(A, 0);
+    for (int g = 0; g < D; g += 2 * WAVE_PF) {
+        bload(B, g + WAVE_PF);
+#pragma unroll
+        for (int s = 0; s < WAVE_PF; ++s)
+            if (g + s < D) bstep(A[s], g + s);
+        bload(A, g + 2 * WAVE_PF);
+#pragma unroll
+        for (int s = 0; s < WAVE_PF; ++s)
+            if (g + WAVE_PF + s < D) bstep(B[s], g + WAVE_PF + s);
+    }
+}
+
 }  // namespace g2
 
 using namespace g2;
@@ -480,6 +699,19 @@ void launch2_advect(const Grid2& g, const Fields2& cur, const Fields2& nxt, cons
 void launch2_cfl(const Grid2& g, const Fields2& F, unsigned long long* out, cudaStream_t st) {
     cudaMemsetAsync(out, 0, sizeof(unsigned long long), st);
     ASTG_LAUNCH(k2_cfl<<<nblk2((long long)g.nx * g.ny), TB2, 0, st>>>(g, F.mx, F.my, out));
+}
+
+void launch2_wave_gather(const Proj& P, const int* vIdx, int rows, cudaStream_t st) {
+    ASTG_LAUNCH(k2_wave_gather<<<nblk2(rows), TB2, 0, st>>>(P, vIdx));
+}
+void launch_precond_wave(const Proj& P, const double* r, double* z, cudaStream_t st) {
+    const int threads = (P.wnx + 31) / 32 * 32;
+    ASTG_LAUNCH(k2_precond_wave<<<1, threads, 0, st>>>(P, r, z));
+    ASTG_LAUNCH(k2_wave_unskew<<<nblk2((long long)P.wnx * P.wny), TB2, 0, st>>>(P, z));
+}
+// the wavefront kernel takes up to WAVE_MAX_NX columns; its diagonal-major slots use 32-bit indices
+bool wave_supported(int nx, int ny) {
+    return nx >= 2 && nx <= WAVE_MAX_NX && (long long)nx * (nx + ny - 1) * 4 < (1LL << 31);
 }
 
 }  // namespace astg

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -61,6 +62,7 @@ struct astg2_handle {
     std::vector<double> subDt;
     std::vector<uint8_t> hostFixed;
     int lastN = 0, lastNnz = 0;
+    bool useWave = false;  // the wavefront MIC(0) sweeps (ASTG_WAVE=0 selects the generic forms)
     astg2_stats last{};
 
     long long nc() const { return (long long)nx * ny; }
@@ -131,6 +133,22 @@ struct astg2_handle {
         d.rho = 2.0;
         proj_alloc(J, nc() + nv(), device, st, allocs);
         J.tolAbsolute = 1;
+        const char* wenv = getenv("ASTG_WAVE");
+        useWave = wave_supported(nx, ny) && !(wenv && std::string(wenv) == "0");
+        if (useWave) {
+            J.wnx = nx;
+            J.wny = ny;
+            const long long skew = (long long)nx * (nx + ny - 1);  // diagonal-major slots
+            J.wRecF = dalloc<double2>(2 * skew);
+            J.wRecB = dalloc<double2>(2 * skew);
+            J.wR = dalloc<double>(skew);
+            J.wZ = dalloc<double>(skew);
+            J.wStatus = status;
+            J.wTt = dalloc<int>(4 * skew);
+            J.wTl = dalloc<double>(4 * skew);
+            J.wTc = dalloc<int>(4 * nv());
+            J.wTv = dalloc<double>(4 * nv());
+        }
         launch2_numbering(g, F[cur], cnt, vIdx, J.bsum, scanTotal, J.nDof, st);
         ck2(cudaStreamSynchronize(st), "init");
     }
@@ -160,9 +178,17 @@ struct astg2_handle {
         select_preconditioner(J, n);
         launch2_assemble(g, d, C, vIdx, J, dt, st);
         bool mixed = precision == ASTG_MIXED && J.pcActive32;
+        // FP64 solves take the wavefront sweeps (one CTA along the anti-diagonals); the mixed form
+        // keeps the FP32 fused preconditioner
+        J.wave = (useWave && !mixed) ? 1 : 0;
+        if (J.wave) J.pcActive = 0;
         launch_factor(d, J, omega, minDiag, epoch, st, &prof);
-        bool owner = mixed || (J.pcActive && J.pcAsync);
-        if (J.clusterSize > 0 || J.pcActive || mixed) launch_level_schedule(d, J, owner, st);
+        if (J.wave) {
+            launch2_wave_gather(J, vIdx, n, st);
+        } else {
+            bool owner = mixed || (J.pcActive && J.pcAsync);
+            if (J.clusterSize > 0 || J.pcActive || mixed) launch_level_schedule(d, J, owner, st);
+        }
         if (mixed) launch_pcg_mixed(d, J, tol, maxIter, 8, st, &prof);
         else launch_pcg_fp64(d, J, tol, maxIter, epoch, 8, st, &prof);
         launch2_correct(g, C, vIdx, J.x, dt, st);

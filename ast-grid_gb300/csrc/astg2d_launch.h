@@ -44,6 +44,10 @@ void launch2_dual(const Grid2& g, const Fields2& F, double* dual, cudaStream_t s
 // adjustLayout (when adaptive) and the three semi-Lagrangian advections, cur -> nxt
 void launch2_advect(const Grid2& g, const Fields2& cur, const Fields2& nxt, const double* dual, const uint8_t* fixedT,
                     bool adaptive, double dt, cudaStream_t st);
+// the wavefront preconditioner's records from the factorised system (Proj::wave fields set);
+// whether the wavefront kernel takes grids nx columns wide
+void launch2_wave_gather(const Proj& P, const int* vIdx, int rows, cudaStream_t st);
+bool wave_supported(int nx, int ny);
 // max over cells of mx(x, y)^2 + my(x, y)^2 (ASTSolver::cfl) as the bit pattern of a double
 void launch2_cfl(const Grid2& g, const Fields2& F, unsigned long long* out, cudaStream_t st);
 

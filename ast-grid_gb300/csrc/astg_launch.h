@@ -150,6 +150,27 @@ struct Proj {
     int* hostDone;   // pinned host
     int tolAbsolute; // 1: the PCG stops at |r|_inf <= tol (the std::vector PCGSolver::solve overload,
                      // include/pcgsolver/pcg_solver.h:302-363); 0: at tol * |b|_inf
+    // wavefront form of the MIC(0) sweeps on a uniform 2-D grid (cells x + y * wnx first, then one
+    // row per open tilt), astg2d.cu.  Per cell, diagonal-major (cell (x, y) at j = x + (x + y) * wnx,
+    // wnx * (wnx + wny - 1) slots), two double2 each:
+    // wRecF = (L to the cell below, L to the cell on the left), (pivot reciprocal, flags);
+    // wRecB = (L from the cell on the right, L from the cell above), (pivot reciprocal, flags); the
+    // flags (an integer in the bits of a double) are 1 below, 2 left, 4 right, 8 above and 16 << k
+    // for corner tilt k of (x, y), (x + 1, y), (x, y + 1), (x + 1, y + 1).  wTt / wTl: those tilts'
+    // rows and entries (4 per cell); wTc / wTv: each tilt row's cells and entries, ascending.
+    // wR: the residual of the cells in the same order (written by the PCG's update), wZ: the
+    // sweeps' result of the cells in that order.
+    int wave;        // 1: precond runs the wavefront kernel
+    int wnx, wny;
+    double2* wRecF;
+    double2* wRecB;
+    double* wR;
+    double* wZ;
+    int* wTt;
+    double* wTl;
+    int* wTc;
+    double* wTv;
+    int* wStatus;    // device status word for wait time-outs
 };
 
 void launch_source(const Dev& d, const Fields& F, cudaStream_t st);
@@ -193,6 +214,8 @@ int choose_dsmem_cluster(bool async, size_t* smemMax);
 void select_preconditioner(Proj& P, int n);
 extern cudaError_t g_cluster_error;  // last failed cluster launch (cudaSuccess if none)
 void launch_factor(const Dev& d, Proj& P, double omega, double minDiag, int& epoch, cudaStream_t st, KProf* prof);
+// the wavefront preconditioner z = (L L^T)^-1 r of a uniform 2-D system (Proj::wave), astg2d.cu
+void launch_precond_wave(const Proj& P, const double* r, double* z, cudaStream_t st);
 int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& epoch, int batch, cudaStream_t st,
                     KProf* prof);
 // mixed-precision PCG (FP32 inner PCG inside FP64 defect correction); returns the outer cycles, or

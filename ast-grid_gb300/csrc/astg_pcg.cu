@@ -1559,6 +1559,18 @@ __global__ void k_to_level_order(Proj P, const double* r) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < *P.nDof) P.rl[P.pos[i]] = r[i];
 }
+// the residual of a cell row in the wavefront preconditioner's diagonal-major order (Proj::wave)
+__device__ __forceinline__ void wave_put_r(const Proj& P, int i, double ri) {
+    const int nx = P.wnx;
+    if (i < nx * P.wny) {
+        const int x = i % nx;
+        P.wR[x + (x + i / nx) * nx] = ri;
+    }
+}
+__global__ void k_to_wave_order(Proj P, const double* r) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *P.nDof) wave_put_r(P, i, r[i]);
+}
 __global__ void k_zero_vec(double* a, const int* nptr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < *nptr) a[i] = 0;
@@ -1653,6 +1665,7 @@ __global__ void k_update_xr(Proj P, double* x, double* r, const double* s, const
         double ri = r[i] + -alpha * z[i];
         r[i] = ri;
         if (P.pcActive) P.rl[P.pos[i]] = ri;
+        if (P.wave) wave_put_r(P, i, ri);
         v = fabs(ri);
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -1721,6 +1734,12 @@ void select_preconditioner(Proj& P, int n) {
     P.pcSmem = bytes;
 }
 static void precond(const Dev& d, Proj& P, const double* r, double* z, int& epoch, cudaStream_t st, KProf* prof) {
+    if (P.wave) {
+        prof_begin(prof, 0, st);
+        launch_precond_wave(P, r, z, st);
+        prof_end(prof, st);
+        return;
+    }
     if (P.pcActive) {
         prof_begin(prof, 0, st);
         cudaError_t e = P.pcAsync ? launch_precond_async(d, P, pca_data64(P), z, P.pcSmem, st)
@@ -1899,6 +1918,7 @@ int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& e
     cudaMemsetAsync(P.done, 0, sizeof(int), st);
     ASTG_LAUNCH(k_absmax<<<nblk(maxRows), TB, 0, st>>>(r, P.nDof, P.amax));
     if (P.pcActive) ASTG_LAUNCH(k_to_level_order<<<nblk(maxRows), TB, 0, st>>>(P, r));
+    if (P.wave) ASTG_LAUNCH(k_to_wave_order<<<nblk(maxRows), TB, 0, st>>>(P, r));
     precond(d, P, r, z, epoch, st, prof);
     ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
     ASTG_LAUNCH(k_pcg_start<<<1, RED_LANES, 0, st>>>(P, P.part, tolFactor));

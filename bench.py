@@ -341,6 +341,56 @@ def adjoint_window(args, device):
     return out
 
 
+def uniform2d(args, device):
+    """The uniform 2-D AST solver (ASTSolver2) on the reference example's configuration
+    (example/ast_smoke_2d/main.cpp: 192 x 384, dt = 0.025f, adaptive tilts): frames per second after
+    a warm-up, device time (CUDA events around each update) and end to end (update plus the
+    getDensity copy to the host), beside the 2-D oracle port on one host core over a short sample
+    of the same frames."""
+    import numpy as np
+
+    import ast_solver
+    from oracle.oracle import Oracle2D
+
+    nx, ny, dt = 192, 384, 0.02500000037252903
+    s = ast_solver.ASTSolver2(resolution=[nx, ny], dx=1.0 / nx, adaptive_dofs=True, name="bench2d", device=device)
+    s.initialize()
+    for _ in range(args.warmup2d):
+        s.update(dt)
+    dev_ms, wall_ms, subs, iters, unknowns = [], [], [], [], []
+    for _ in range(args.frames2d):
+        w0 = time.perf_counter()
+        s.update(dt)
+        d = s.getDensity()
+        wall_ms.append(1e3 * (time.perf_counter() - w0))
+        st = s.last_stats()
+        dev_ms.append(st["ms"])
+        subs.append(st["substeps"])
+        iters.append(st["pcg_iterations"])
+        unknowns.append(st["unknowns"])
+    s.close()
+    out = {"workload": f"ASTSolver2 {nx}x{ny}, dt 0.025f, adaptive tilts, frames {args.warmup2d + 1}.."
+                       f"{args.warmup2d + args.frames2d}",
+           "value": 1e3 / float(np.mean(dev_ms)), "unit": "frames/s", "ms_per_frame": float(np.mean(dev_ms)),
+           "e2e": {"value": 1e3 / float(np.mean(wall_ms)), "unit": "frames/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 8 * nx * ny},
+           "substeps_mean": float(np.mean(subs)), "unknowns_mean": float(np.mean(unknowns)),
+           "pcg_iters_last_substep_mean": float(np.mean(iters)), "density_sum": float(d.sum())}
+    if args.cpu_frames2d > 0:
+        o = Oracle2D(nx, ny, adaptive=True, reduce_mode=0)
+        for _ in range(args.warmup2d):
+            o.update(dt)
+        c0 = time.perf_counter()
+        for _ in range(args.cpu_frames2d):
+            o.update(dt)
+        cpu_s = (time.perf_counter() - c0) / args.cpu_frames2d
+        o.close()
+        out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "frames/s", "cores": 1, "kind": "port",
+                               "sample": f"{args.cpu_frames2d} frames after the same {args.warmup2d}-frame warm-up, "
+                                         "2-D oracle in the reference's arithmetic order"}
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if ws > 1 and rank != 0:
@@ -522,6 +572,9 @@ def run_ours(args):
     comparison = None
     if rank == 0 and args.compare_steps > 0:
         comparison = precision_comparison(args, local)
+    flat2d = None
+    if rank == 0 and args.frames2d > 0:
+        flat2d = uniform2d(args, local)
 
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
@@ -533,7 +586,7 @@ def run_ours(args):
             "wall_ms_per_step": 1e3 * wall / args.steps,
             "roofline": roofline, "kernels": kernel_breakdown, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clocks, "gpu_launches": launches, "isolated_solves": solves, "adjoint": adjoint,
-            "precision_comparison": comparison}
+            "precision_comparison": comparison, "uniform2d": flat2d}
     s.close()
     D.barrier()
     if rank == 0:
@@ -556,6 +609,9 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=128, help="steps of the differentiated window (0: skip)")
     ap.add_argument("--adjoint-every", type=int, default=16, help="checkpoint interval of the adjoint tape")
     ap.add_argument("--compare-steps", type=int, default=50, help="steps of the FP64 / mixed comparison (0: skip)")
+    ap.add_argument("--frames2d", type=int, default=20, help="timed frames of the uniform 2-D solver (0: skip)")
+    ap.add_argument("--warmup2d", type=int, default=10, help="warm-up frames of the uniform 2-D solver")
+    ap.add_argument("--cpu-frames2d", type=int, default=2, help="frames of the 2-D oracle CPU sample (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
