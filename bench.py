@@ -612,11 +612,15 @@ def main():
     ap.add_argument("--frames2d", type=int, default=20, help="timed frames of the uniform 2-D solver (0: skip)")
     ap.add_argument("--warmup2d", type=int, default=10, help="warm-up frames of the uniform 2-D solver")
     ap.add_argument("--cpu-frames2d", type=int, default=2, help="frames of the 2-D oracle CPU sample (0: skip)")
+    ap.add_argument("--only-2d", action="store_true", help="run only the uniform 2-D solver section and print it")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
         return run_reference(args)
+    if args.only_2d:
+        print(json.dumps({"uniform2d": uniform2d(args, 0)}), flush=True)
+        return 0
     return run_ours(args)
 
 
