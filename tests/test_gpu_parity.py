@@ -153,18 +153,21 @@ def test_every_sweep_form_bit_identical_to_oracle(mode, monkeypatch):
     s.close()
 
 
-def test_full_benchmark_size_step_bit_identical_to_oracle():
-    """256^3-equivalent octree (64^3 coarsest, 3 levels), the size the benchmark runs: one step."""
+def test_full_benchmark_size_steps_bit_identical_to_oracle():
+    """256^3-equivalent octree (64^3 coarsest, 3 levels), the size the benchmark runs: ten steps,
+    every field, the pressure and the iteration count after each (200 steps were checked the same
+    way once; ten keep the suite short)."""
     from oracle.oracle import Oracle
 
     s = solver(64, 3)
     o = Oracle(64, 3, reduce_mode=1, openmp=True)
-    s.update(DT)
-    o.step(DT)
-    assert s.size(7) > 200  # the barrier-free fused preconditioner ran
-    assert s.last_solve().iterations == int(o.get("pcg_iters")[0])
-    for f in ["density_oct", "heat_oct", "mac", "tilt_vel", "dual_oct", "tilt_open", "p"]:
-        assert_same(f"step1/{f}", o.get(f), s.get(f))
+    for k in range(1, 11):
+        s.update(DT)
+        o.step(DT)
+        assert s.size(7) > 200  # the barrier-free fused preconditioner ran
+        assert s.last_solve().iterations == int(o.get("pcg_iters")[0]), f"step {k}"
+        for f in ["density_oct", "density_tilt", "heat_oct", "mac", "tilt_vel", "dual_oct", "tilt_open", "p"]:
+            assert_same(f"step{k}/{f}", o.get(f), s.get(f))
     s.close()
 
 
