@@ -66,6 +66,7 @@ struct astg_handle {
     std::string err;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evA = nullptr, evB = nullptr;
+    cudaEvent_t evF0 = nullptr, evF1 = nullptr, evAdv = nullptr;  // stage boundaries of astg_step
 
     // ---------------------------------------------------------------- topology (host)
     int L = 0, res = 0, S = 0, H = 0;
@@ -123,7 +124,7 @@ struct astg_handle {
         freeTape();
         for (void* p : allocs) cudaFree(p);
         if (J.hostDone) cudaFreeHost(J.hostDone);
-        for (cudaEvent_t e : {ev0, ev1, evA, evB})
+        for (cudaEvent_t e : {ev0, ev1, evA, evB, evF0, evF1, evAdv})
             if (e) cudaEventDestroy(e);
         if (st) cudaStreamDestroy(st);
     }
@@ -404,7 +405,7 @@ struct astg_handle {
             if (v < 0 || v >= L) throw std::invalid_argument("split map holds a level outside [0, levels)");
         ck(cudaSetDevice(P.device), "cudaSetDevice");
         ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
-        for (cudaEvent_t* e : {&ev0, &ev1, &evA, &evB}) ck(cudaEventCreate(e), "event");
+        for (cudaEvent_t* e : {&ev0, &ev1, &evA, &evB, &evF0, &evF1, &evAdv}) ck(cudaEventCreate(e), "event");
 
         buildLayout();
         buildTables();
@@ -1051,6 +1052,9 @@ struct astg_handle {
         if (T.on && T.recording) advDst = tapeBeforeStep(dt);
         for (int i = 0; i < 6; ++i) {
             if (i == 5 && advDst) saveAdvectionInput(advDst);
+            if (i == 1) ck(cudaEventRecord(evF0, st), "event");
+            if (i == 3) ck(cudaEventRecord(evF1, st), "event");
+            if (i == 5) ck(cudaEventRecord(evAdv, st), "event");
             stage(i, dt);
         }
         if (T.on && T.recording) ++T.steps;
@@ -1059,11 +1063,14 @@ struct astg_handle {
         if (out) {
             float ms = 0;
             cudaEventElapsedTime(&ms, ev0, ev1);
+            float msF = 0, msA = 0;
+            cudaEventElapsedTime(&msF, evF0, evF1);
+            cudaEventElapsedTime(&msA, evAdv, ev1);
             out->solve = last;
             out->ms_total = ms;
             out->ms_project = last.ms;
-            out->ms_force = 0;
-            out->ms_advect = 0;
+            out->ms_force = msF;
+            out->ms_advect = msA;
         }
     }
 

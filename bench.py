@@ -443,6 +443,7 @@ def run_ours(args):
     pcg_ms = []
     dofs = []
     nnzs = []
+    adv_ms = []
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         D.barrier()
@@ -451,6 +452,7 @@ def run_ours(args):
             s.update(DT)
             st = s.last_step
             dev_ms.append(st.ms_total)
+            adv_ms.append(st.ms_advect)
             iters.append(st.solve.iterations)
             pcg_ms.append(st.solve.ms)
             dofs.append(st.solve.n)
@@ -559,6 +561,14 @@ def run_ours(args):
                 "preconditioner_form": form}
     kernel_breakdown = {names[k]: {"avg_launch_ms": avg[k], "timed_launches": kms[k][1],
                                    "est_ms_per_step": avg[k] * per_step[k]} for k in avg}
+    # advection stage (tilt adaptivity, scalars, faces, tilts, half tilts, decay) against its
+    # compulsory traffic: 176 B read + 120 B written per slot (no SDF grid: the scene has no collider)
+    adv_bytes = 296.0 * S
+    adv_mean = float(np.mean(adv_ms))
+    advection = {"algorithmic_bytes_per_step": adv_bytes, "ms_per_step": adv_mean,
+                 "achieved_GBps": adv_bytes / (adv_mean / 1e3) / 1e9 if adv_mean > 0 else None,
+                 "frac": (adv_bytes / (adv_mean / 1e3) / 1e9) / peak if adv_mean > 0 else None,
+                 "note": "gather- and FP64-latency-bound sampling (2 RK2 velocity samples per advected point)"}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -584,7 +594,7 @@ def run_ours(args):
                        "l2": "state larger than L2 (no flush)", "parallelism": f"replicas x{ws}"},
             "pcg_ms_per_solve": float(np.mean(pcg_ms)), "pcg_iters_mean": float(np.mean(iters)), "mixed": mixed,
             "wall_ms_per_step": 1e3 * wall / args.steps,
-            "roofline": roofline, "kernels": kernel_breakdown, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roofline, "kernels": kernel_breakdown, "advection": advection, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clocks, "gpu_launches": launches, "isolated_solves": solves, "adjoint": adjoint,
             "precision_comparison": comparison, "uniform2d": flat2d}
     s.close()

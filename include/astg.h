@@ -76,7 +76,9 @@ typedef struct astg_solve_stats {
 typedef struct astg_step_stats {
     astg_solve_stats solve;
     double ms_total;      /* device time of the whole step */
-    double ms_force, ms_project, ms_advect;
+    double ms_force;      /* device time of addForce and the wall / ghost constraint after it */
+    double ms_project;    /* the projection's PCG solve (its astg_solve_stats.ms) */
+    double ms_advect;     /* tilt adaptivity, the advection of scalars and velocity, the decay */
 } astg_step_stats;
 
 /* Fills p with the benchmark defaults for a given coarsest resolution and level count. */
