@@ -236,10 +236,13 @@ def isolated_solves(args, device):
 
 
 def precision_comparison(args, device):
-    """The mixed form against the FP64 form on the benchmark scene: two handles from the same
-    initial state step side by side; per step the relative L2 difference of the octagon density and
-    of the pressure, and each form's final relative residual |b - A p|_inf / |b|_inf of its solve
-    (both stop at 1e-6)."""
+    """The mixed form against the FP64 form on the benchmark scene (200 steps by default, the length
+    of the three-way comparison; the FP64 form is bit-identical to the FP64 oracle, so its numbers
+    are also the mixed form's errors against the oracle): two handles from the same initial state
+    step side by side; per step the relative L2 difference of the octagon density and of the
+    pressure, and each form's final relative residual |b - A p|_inf / |b|_inf of its solve (both
+    stop at 1e-6): b - A p is the projected velocity's discrete divergence (times rho / dt), so this
+    is the divergence left after the projection relative to the divergence before it."""
     import numpy as np
 
     import ast_solver
@@ -264,7 +267,8 @@ def precision_comparison(args, device):
                       "mixed form (separate handles)",
             "density_rel_l2_mixed_vs_fp64": pick(dens), "pressure_rel_l2_mixed_vs_fp64": pick(pres),
             "rel_residual_fp64": pick(ra), "rel_residual_mixed": pick(rb),
-            "per_step_density": dens}
+            "per_step_density": dens, "per_step_pressure": pres, "per_step_divergence_fp64": ra,
+            "per_step_divergence_mixed": rb}
 
 
 def adjoint_window(args, device):
@@ -618,7 +622,7 @@ def main():
     ap.add_argument("--solve-rhs", type=int, default=20, help="right-hand sides of the isolated solves (0: skip)")
     ap.add_argument("--adjoint-steps", type=int, default=128, help="steps of the differentiated window (0: skip)")
     ap.add_argument("--adjoint-every", type=int, default=16, help="checkpoint interval of the adjoint tape")
-    ap.add_argument("--compare-steps", type=int, default=50, help="steps of the FP64 / mixed comparison (0: skip)")
+    ap.add_argument("--compare-steps", type=int, default=200, help="steps of the FP64 / mixed comparison (0: skip)")
     ap.add_argument("--frames2d", type=int, default=20, help="timed frames of the uniform 2-D solver (0: skip)")
     ap.add_argument("--warmup2d", type=int, default=10, help="warm-up frames of the uniform 2-D solver")
     ap.add_argument("--cpu-frames2d", type=int, default=2, help="frames of the 2-D oracle CPU sample (0: skip)")
