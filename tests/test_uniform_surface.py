@@ -65,3 +65,18 @@ def test_benchmark_module_functions():
     ast_solver.benchmark_stop_timer_section("a")
     ast_solver.benchmark_report(include_messages=True)
     ast_solver.benchmark_reset()
+
+
+def test_solver2_without_a_device_fails_loudly():
+    """No CUDA device (this CPU host): ASTSolver2 raises instead of falling back to anything."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    try:
+        ast_solver.lib()
+    except OSError:
+        pytest.skip("the CUDA library is not built here")
+    s = ast_solver.ASTSolver2(resolution=[16, 32], dx=1.0 / 16, adaptive_dofs=True, name="cpu")
+    with pytest.raises(ast_solver.AstgError) as e:
+        s.initialize()
+    assert e.value.status == ast_solver.ASTG_NO_DEVICE
