@@ -31,6 +31,7 @@ void ck2(cudaError_t e, const char* what) {
 constexpr double SQRT2_H = 1.4142135623730951;  // include/macro.h:16
 constexpr double EPS_H = 2.220446049250313e-16;  // include/general.h:48
 constexpr long long MAX_ROWS_2D = 2048LL * 2048LL;
+constexpr int MAX_SUBSTEPS_2D = 100000;  // per astg2_update
 
 }  // namespace
 
@@ -261,6 +262,10 @@ struct astg2_handle {
         int subs = 0;
         while (remaining > EPS_H) {
             int n = numberOfSubTimeSteps(remaining);
+            // the reference would run them all; a frame this split has a diverged velocity field
+            if (n > MAX_SUBSTEPS_2D)
+                throw std::runtime_error("CFL asks for " + std::to_string(n) +
+                                         " sub-steps in one frame: the velocity diverged");
             double actual = remaining / (double)n;
             substep(actual);
             ++subs;

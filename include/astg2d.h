@@ -57,7 +57,9 @@ astg_status astg2_create(int nx, int ny, double dx, int adaptive_dofs, int devic
 void astg2_destroy(astg2_handle* h);
 const char* astg2_last_error(const astg2_handle* h);
 
-/* Solver::update(dt) (src/solver.cpp:8-46): CFL sub-steps of source, force, project, advect */
+/* Solver::update(dt) (src/solver.cpp:8-46): CFL sub-steps of source, force, project, advect.
+ * ASTG_NAN_DETECTED when the CFL number is not finite or asks for more than 100,000 sub-steps in
+ * one call (a diverged velocity field; the reference would keep stepping). */
 astg_status astg2_update(astg2_handle* h, double dt);
 /* one stage of a sub-step: 0 sphereSource2DSetup, 1 addForce, 2 project, 3 advect, 4 all four */
 astg_status astg2_stage(astg2_handle* h, int stage, double dt);
