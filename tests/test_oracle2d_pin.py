@@ -93,3 +93,40 @@ def test_oracle2d_rejects_bad_arguments():
         o.get("no_such_field")
     with pytest.raises(RuntimeError):
         o.set("p", np.zeros(3))
+
+
+def test_substep_is_the_four_stages_in_order():
+    """onUpdate = sphereSource2DSetup, addForce, project, advect: one sub-step equals the four
+    stages run one by one, bit for bit."""
+    a, b = orc.Oracle2D(24, 48, adaptive=True), orc.Oracle2D(24, 48, adaptive=True)
+    for _ in range(3):
+        a.stage("substep", 0.02)
+        for st in STAGES:
+            b.stage(st, 0.02)
+    for f in STATE + OPEN_ONLY:
+        np.testing.assert_array_equal(a.get(f), b.get(f), err_msg=f)
+
+
+def test_non_adaptive_layout_never_opens():
+    o = orc.Oracle2D(24, 48, adaptive=False)
+    for _ in range(4):
+        o.update(0.025)
+    assert o.get("tilt_open").sum() == 0
+    assert (o.get("pindex_vert") == -1).all()
+    assert o.info()["unknowns"] == 24 * 48
+
+
+def test_boundary_tilts_stay_closed_and_cells_keep_their_numbers():
+    o = orc.Oracle2D(32, 64, adaptive=True)
+    for _ in range(4):
+        o.update(0.025)
+    op = o.get("tilt_open")
+    assert op.sum() > 0
+    assert op[0, :].sum() == op[-1, :].sum() == op[:, 0].sum() == op[:, -1].sum() == 0
+    np.testing.assert_array_equal(o.get("pindex_cell").ravel(), np.arange(32 * 64))
+    # the tilts of the last projection's layout (the one before the last advection, as in the
+    # reference, whose updateIndex runs in project) are numbered after the cells in vertex order
+    pv = o.get("pindex_vert").ravel()
+    numbered = pv[pv >= 0]
+    assert len(numbered) > 0
+    np.testing.assert_array_equal(numbered, np.arange(32 * 64, 32 * 64 + len(numbered)))
