@@ -13,9 +13,10 @@
 // evaluates the difference the expression spells out.
 //
 // Kernels per sub-step: source, force (+ x walls), numbering (scan of the open tilts), assembly of
-// padded rows -> CSR (shared with the octree path), MIC(0)-PCG (shared), pressure correction
-// (+ x walls), dual velocities, and one fused advection kernel (layout adjustment, density, heat,
-// tilted faces and MAC faces; density and heat share each back-trace).
+// padded rows -> CSR (shared with the octree path), MIC(0) factorisation and PCG (shared; the
+// preconditioner is the wavefront kernel below), pressure correction (+ x walls), dual velocities,
+// and one fused advection kernel (layout adjustment, density, heat, tilted faces and MAC faces;
+// density and heat share each back-trace).
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -435,7 +436,6 @@ __global__ void k2_cfl(Grid2 g, const double* mx, const double* my, unsigned lon
     if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
 }
 
-
 // ------------------------------------------------------------------ wavefront MIC(0) sweeps
 // The system's cells come first in raster order, so a cell's lower neighbours are the cells below
 // and to the left (one anti-diagonal earlier) and its upper ones the cells to the right and above
@@ -452,8 +452,10 @@ __global__ void k2_cfl(Grid2 g, const double* mx, const double* my, unsigned lon
 // result (a warp shuffle), across a warp boundary a shared-memory slot per warp and step parity.
 // The per-cell records, the residual and the results are stored diagonal-major (cell (x, y) at
 // x + (x + y) * nx), so every step's accesses are contiguous across a warp; they are loaded WAVE_PF
-// steps ahead.  A second kernel returns the cells' result to the system's order.  (A barrier-free form with per-warp progress counters measured 1.5x slower: its per-step
-// handshake and fences cost more than the barrier.)
+// steps ahead.  A second kernel returns the cells' result to the system's order.  Each step's
+// critical path is three dependent FP64 operations (~60 cycles each on this GPU) plus a shuffle
+// and the barrier.  (A barrier-free form with per-warp progress counters measured 1.5x slower:
+// its per-step handshake and fences cost more than the barrier.)
 constexpr int WAVE_PF = 4;
 constexpr int WAVE_MAX_NX = 512;
 constexpr int WAVE_MAX_W = WAVE_MAX_NX / 32;
