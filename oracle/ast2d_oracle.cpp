@@ -748,13 +748,16 @@ extern "C" {
 
 const char* ast2o_error() { return g_err.c_str(); }
 
-void* ast2o_create(int nx, int ny, double dx, int adaptive, int reduceMode) {
-    if (nx < 2 || ny < 2 || !(dx > 0)) {
-        g_err = "2-D oracle: resolution must be at least 2x2 and dx positive";
+// workers: the reference's taskflow worker count (its default is the host's hardware threads,
+// src/util.cpp:10), which sets the slices of its dot products in reduce mode 0
+void* ast2o_create(int nx, int ny, double dx, int adaptive, int reduceMode, int workers) {
+    if (nx < 2 || ny < 2 || !(dx > 0) || workers < 1) {
+        g_err = "2-D oracle: resolution must be at least 2x2, dx positive, workers at least 1";
         return nullptr;
     }
     Solver2* s = new Solver2(nx, ny, dx, adaptive != 0);
     s->pcg.reduceMode = reduceMode;
+    s->pcg.workers = workers;
     s->initialize();
     return s;
 }

@@ -193,7 +193,7 @@ def lib2d():
         L = ctypes.CDLL(build2d())
         L.ast2o_error.restype = ctypes.c_char_p
         L.ast2o_create.restype = ctypes.c_void_p
-        L.ast2o_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.ast2o_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.ast2o_destroy.argtypes = [ctypes.c_void_p]
         L.ast2o_update.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.ast2o_stage.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
@@ -214,14 +214,16 @@ STAGES2D = {"source": 0, "force": 1, "project": 2, "advect": 3, "substep": 4}
 class Oracle2D:
     """The uniform 2-D AST smoke solver (ASTSolver<2>, sphere source at the bottom, closed x walls,
     open top and bottom) on an nx x ny grid of spacing dx.  reduce_mode 0 follows the reference's
-    arithmetic order (per-worker dot slices over 8 workers), 1 the CUDA library's (fixed
-    reduction tree, fused multiply-subtract in the MIC(0) sweeps)."""
+    arithmetic order (its dot products summed in per-worker slices over ref_workers taskflow
+    workers -- the reference's default is the host's hardware thread count; the committed
+    fixtures came from an 8-thread host), 1 the CUDA library's (fixed reduction tree, fused
+    multiply-subtract in the MIC(0) sweeps)."""
 
-    def __init__(self, nx, ny, dx=None, adaptive=True, reduce_mode=0):
+    def __init__(self, nx, ny, dx=None, adaptive=True, reduce_mode=0, ref_workers=8):
         self._lib = lib2d()
         self.nx, self.ny = nx, ny
         self.dx = 1.0 / nx if dx is None else dx
-        self._h = self._lib.ast2o_create(nx, ny, self.dx, 1 if adaptive else 0, reduce_mode)
+        self._h = self._lib.ast2o_create(nx, ny, self.dx, 1 if adaptive else 0, reduce_mode, ref_workers)
         if not self._h:
             raise ValueError(self._lib.ast2o_error().decode())
 

@@ -35,7 +35,10 @@ first frames (stages source, force, project, advect; project also holds A_rowptr
 b, p), substeps (per frame) and sub_dt.  The "stock" cases run the reference as it is; the "eval"
 cases run ref_harness2d_eval, which evaluates the correction term of ASTFaceGrid<double, 2>::sample
 that the stock code reads from a destroyed temporary (see ref_harness2d.cpp).  Values of closed
-tilts are stale pool memory in the reference and are not meaningful.
+tilts are stale pool memory in the reference and are not meaningful.  The reference sums its PCG
+dot products in slices of its taskflow workers, one per hardware thread of the host: the
+committed fixtures came from an 8-thread host, which the 2-D oracle's ref_workers default
+(8) matches; regenerating them elsewhere needs the same worker count on both sides.
 
     python tests/golden/make_golden.py --2d-only
 """
