@@ -2,8 +2,11 @@
 reference's pybind module ``ast_solver``, python_bindings/ast_solver.cc:14-80).
 
 ``OctreeSmoke3`` wraps OctreeOmniGridSolver3 (include/octree_omnigrid_solver3.h:23-57) through
-the C ABI of include/astg.h.  The library must be built (``build_lib.build()``); importing this
-module on a machine without it raises instead of falling back to anything.
+the C ABI of include/astg.h; ``ASTSolver2`` runs the reference module's uniform 2-D solver
+(ASTSolver<2>, include/ast_solver.h) through include/astg2d.h, and the module's other bound names
+(``ASTGridLayout2/3``, ``TiltNode2/3``, ``CellNode2/3``, ``ASTGrid2/3``, ``ASTSolver3``,
+``benchmark_*``) keep their signatures.  The library must be built (``build_lib.build()``); using
+a solver on a machine without it raises instead of falling back to anything.
 """
 import ctypes
 import os
