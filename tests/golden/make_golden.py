@@ -41,6 +41,9 @@ committed fixtures came from an 8-thread host, which the 2-D oracle's ref_worker
 (8) matches; regenerating them elsewhere needs the same worker count on both sides.
 
     python tests/golden/make_golden.py --2d-only
+
+The same command writes ref2d_eval_a192_hashes.json: the reference example's full size (192 x 384,
+evaluated correction term, 6 frames) pinned by the sha256 of every array of every frame.
 """
 import os
 import subprocess
@@ -78,6 +81,48 @@ CASES2D = [
     ("ref2d_eval_a32_substeps", "ref_harness2d_eval", 32, 64, 3, 0.3, 1, 0),
 ]
 DROP2D = ("dual_vert",)
+# full-size pins as hashes (the arrays themselves are too large to commit): the reference example's
+# 192 x 384 with the evaluated correction term, every frame of a short run
+HASH2D = [
+    # name, harness, nx, ny, frames, dt, adaptive
+    ("ref2d_eval_a192_hashes", "ref_harness2d_eval", 192, 384, 6, 0.02500000037252903, 1),
+]
+HASH_FIELDS = ["density_cell", "heat_cell", "mac_x", "mac_y", "tilt_open", "pindex_cell", "pindex_vert"]
+HASH_OPEN_ONLY = ["density_vert", "heat_vert", "tilt_vel"]
+
+
+def frame_hashes(get, is_open):
+    """sha256 of each array's bytes (little-endian, the reference's order); the tilt-vertex fields
+    only where the tilt is open (closed tilts hold stale pool memory in the reference)."""
+    import hashlib
+
+    out = {}
+    for f in HASH_FIELDS:
+        out[f] = hashlib.sha256(np.ascontiguousarray(get(f)).tobytes()).hexdigest()
+    for f in HASH_OPEN_ONLY:
+        out[f] = hashlib.sha256(np.ascontiguousarray(get(f)[is_open]).tobytes()).hexdigest()
+    return out
+
+
+def hashes_2d():
+    import json
+
+    for name, exe, nx, ny, frames, dt, adaptive in HASH2D:
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "out.astg")
+            subprocess.check_call([os.path.join(ROOT, "oracle", "_ref", exe), str(nx), str(ny), str(frames), repr(dt),
+                                   str(adaptive), path, "0"], stdout=subprocess.DEVNULL)
+            R = astg_archive.read(path)
+            rec = {"case": [nx, ny, frames, adaptive], "dt": dt, "substeps": R["substeps"].tolist(),
+                   "sub_dt": [float(v).hex() for v in R["sub_dt"]], "frames": []}
+            for f in range(1, frames + 1):
+                p = f"f{f}/"
+                is_open = R[p + "tilt_open"].astype(bool)
+                rec["frames"].append(frame_hashes(lambda k: R[p + k], is_open))
+            dst = os.path.join(HERE, name + ".json")
+            with open(dst, "w") as fh:
+                json.dump(rec, fh, indent=1)
+            print(f"{dst}: {os.path.getsize(dst) / 1e3:.1f} kB")
 
 
 def fixtures_2d():
@@ -147,6 +192,7 @@ def main():
     harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
     if "--2d-only" in sys.argv:
         fixtures_2d()
+        hashes_2d()
         return
     if "--ckpt-only" not in sys.argv:
         extrap_fixtures(harness)

@@ -145,3 +145,29 @@ def test_worker_count_only_changes_the_dot_summation():
     np.testing.assert_array_equal(a.get("mac_y"), R["f3/mac_y"])
     assert not np.array_equal(b.get("mac_y"), R["f3/mac_y"])
     np.testing.assert_allclose(b.get("mac_y"), R["f3/mac_y"], rtol=0, atol=1e-9)
+
+
+def test_oracle2d_matches_reference_at_the_example_size():
+    """The reference example's full size (192 x 384, dt 0.025f, adaptive, correction term
+    evaluated): six frames of the oracle hash to the reference's own arrays, every field of every
+    frame, with the same CFL sub-steps."""
+    import json
+    import os as _os
+    import sys as _sys
+
+    _sys.path.insert(0, GOLDEN)
+    import make_golden
+
+    rec = json.load(open(_os.path.join(GOLDEN, "ref2d_eval_a192_hashes.json")))
+    nx, ny, frames, adaptive = rec["case"]
+    o = orc.Oracle2D(nx, ny, adaptive=bool(adaptive))
+    subs = []
+    for f in range(frames):
+        o.update(rec["dt"])
+        subs.append(o.info()["substeps"])
+        is_open = o.get("tilt_open").astype(bool)
+        got = make_golden.frame_hashes(o.get, is_open)
+        assert got == rec["frames"][f], f"frame {f + 1}: " + ", ".join(
+            k for k in got if got[k] != rec["frames"][f][k])
+    assert subs == rec["substeps"]
+    assert [float(v).hex() for v in o.get("sub_dt")] == rec["sub_dt"]
