@@ -42,7 +42,13 @@ committed fixtures came from an 8-thread host, which the 2-D oracle's ref_worker
 
     python tests/golden/make_golden.py --2d-only
 
-The same command writes ref2d_eval_a192_hashes.json: the reference example's full size (192 x 384,
+Config 0 at its full length (32^3 coarsest x 3 levels, 50 steps) pinned by the sha256 of every
+state array, the DOF maps, the pressure and the iteration count after every step
+(ref_c32_l3_hashes.json):
+
+    python tests/golden/make_golden.py --hashes-3d
+
+The 2-D command also writes ref2d_eval_a192_hashes.json: the reference example's full size (192 x 384,
 evaluated correction term, 6 frames) pinned by the sha256 of every array of every frame.
 """
 import os
@@ -102,6 +108,36 @@ def frame_hashes(get, is_open):
     for f in HASH_OPEN_ONLY:
         out[f] = hashlib.sha256(np.ascontiguousarray(get(f)[is_open]).tobytes()).hexdigest()
     return out
+
+
+# config 0's full length pinned by hashes: 32^3 coarsest x 3 levels, 50 steps
+HASH3D = [("ref_c32_l3_hashes", 32, 3, 50)]
+HASH3D_FIELDS = ["density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
+                 "tilt_e", "tilt_flags", "tilt_open", "pindex_oct", "pindex_tilt", "p", "pcg_iters"]
+
+
+def step_hashes(get):
+    """sha256 of each array's bytes (the reference's slot order)."""
+    import hashlib
+
+    return {f: hashlib.sha256(np.ascontiguousarray(get(f)).tobytes()).hexdigest() for f in HASH3D_FIELDS}
+
+
+def hashes_3d(harness):
+    import json
+
+    for name, c, lv, steps in HASH3D:
+        with tempfile.TemporaryDirectory() as d:
+            subprocess.check_call([harness, "--coarsest", str(c), "--levels", str(lv), "--steps", str(steps), "--out", d],
+                                  stdout=subprocess.DEVNULL)
+            rec = {"case": [c, lv, steps], "dt": 0.01, "steps": []}
+            for k in range(1, steps + 1):
+                st = astg_archive.read(os.path.join(d, f"step_{k:04d}.astg"))
+                rec["steps"].append(step_hashes(lambda f: st[f]))
+            dst = os.path.join(HERE, name + ".json")
+            with open(dst, "w") as fh:
+                json.dump(rec, fh, indent=1)
+            print(f"{dst}: {os.path.getsize(dst) / 1e3:.1f} kB")
 
 
 def hashes_2d():
@@ -190,6 +226,9 @@ def main():
     subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref", "Makefile"), f"REF={ref}",
                            "-j8"])
     harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+    if "--hashes-3d" in sys.argv:
+        hashes_3d(harness)
+        return
     if "--2d-only" in sys.argv:
         fixtures_2d()
         hashes_2d()

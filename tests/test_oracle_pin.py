@@ -105,3 +105,26 @@ def test_extrapolation_bit_exact(name):
     assert_same("after/density_tilt", g["after/density_tilt"], o.get("density_tilt"))
     changed = np.sum(g["after/density_oct"] != before["density_oct"]) + np.sum(g["after/density_tilt"] != before["density_tilt"])
     assert changed > 50
+
+
+def test_config0_full_length_hashes_match_reference():
+    """Config 0 at its full length (32^3 coarsest x 3 levels, 50 steps): after every step the oracle
+    (reference reduction order) hashes to the reference's own arrays -- every state field, the tilt
+    layout, the DOF maps, the pressure and the PCG iteration count."""
+    import json
+    import os
+    import sys
+
+    from fixtures import GOLDEN
+
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+
+    rec = json.load(open(os.path.join(GOLDEN, "ref_c32_l3_hashes.json")))
+    c, lv, steps = rec["case"]
+    o = Oracle(c, lv, openmp=True)
+    for k in range(steps):
+        o.step(rec["dt"])
+        got = make_golden.step_hashes(o.get)
+        bad = [f for f in got if got[f] != rec["steps"][k][f]]
+        assert not bad, f"step {k + 1}: {bad}"
