@@ -42,9 +42,9 @@ committed fixtures came from an 8-thread host, which the 2-D oracle's ref_worker
 
     python tests/golden/make_golden.py --2d-only
 
-Config 0 at its full length (32^3 coarsest x 3 levels, 50 steps) pinned by the sha256 of every
-state array, the DOF maps, the pressure and the iteration count after every step
-(ref_c32_l3_hashes.json):
+Config 0 at its full length (32^3 coarsest x 3 levels, 50 steps) and the benchmark size (64^3 x 3,
+20 steps) pinned by the sha256 of every state array, the DOF maps, the pressure and the iteration
+count after every step (ref_c32_l3_hashes.json, ref_c64_l3_hashes.json):
 
     python tests/golden/make_golden.py --hashes-3d
 
@@ -111,7 +111,9 @@ def frame_hashes(get, is_open):
 
 
 # config 0's full length pinned by hashes: 32^3 coarsest x 3 levels, 50 steps
-HASH3D = [("ref_c32_l3_hashes", 32, 3, 50)]
+HASH3D = [("ref_c32_l3_hashes", 32, 3, 50),
+          # the benchmark size (config 1's 256^3-equivalent), its first 20 steps
+          ("ref_c64_l3_hashes", 64, 3, 20)]
 HASH3D_FIELDS = ["density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
                  "tilt_e", "tilt_flags", "tilt_open", "pindex_oct", "pindex_tilt", "p", "pcg_iters"]
 

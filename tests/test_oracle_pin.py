@@ -107,10 +107,12 @@ def test_extrapolation_bit_exact(name):
     assert changed > 50
 
 
-def test_config0_full_length_hashes_match_reference():
-    """Config 0 at its full length (32^3 coarsest x 3 levels, 50 steps): after every step the oracle
-    (reference reduction order) hashes to the reference's own arrays -- every state field, the tilt
-    layout, the DOF maps, the pressure and the PCG iteration count."""
+@pytest.mark.parametrize("name", ["ref_c32_l3_hashes", "ref_c64_l3_hashes"])
+def test_full_size_hashes_match_reference(name):
+    """Config 0 at its full length (32^3 coarsest x 3 levels, 50 steps) and the benchmark size (64^3
+    x 3 levels, 20 steps): after every step the oracle (reference reduction order) hashes to the
+    reference's own arrays -- every state field, the tilt layout, the DOF maps, the pressure and
+    the PCG iteration count."""
     import json
     import os
     import sys
@@ -120,7 +122,7 @@ def test_config0_full_length_hashes_match_reference():
     sys.path.insert(0, GOLDEN)
     import make_golden
 
-    rec = json.load(open(os.path.join(GOLDEN, "ref_c32_l3_hashes.json")))
+    rec = json.load(open(os.path.join(GOLDEN, name + ".json")))
     c, lv, steps = rec["case"]
     o = Oracle(c, lv, openmp=True)
     for k in range(steps):
