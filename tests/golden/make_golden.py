@@ -92,6 +92,8 @@ DROP2D = ("dual_vert",)
 HASH2D = [
     # name, harness, nx, ny, frames, dt, adaptive
     ("ref2d_eval_a192_hashes", "ref_harness2d_eval", 192, 384, 6, 0.02500000037252903, 1),
+    # the stock reference without adaptivity (never reaches the sampler's destroyed temporary)
+    ("ref2d_stock_n192_hashes", "ref_harness2d", 192, 384, 6, 0.02500000037252903, 0),
 ]
 HASH_FIELDS = ["density_cell", "heat_cell", "mac_x", "mac_y", "tilt_open", "pindex_cell", "pindex_vert"]
 HASH_OPEN_ONLY = ["density_vert", "heat_vert", "tilt_vel"]

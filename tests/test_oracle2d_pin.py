@@ -147,10 +147,11 @@ def test_worker_count_only_changes_the_dot_summation():
     np.testing.assert_allclose(b.get("mac_y"), R["f3/mac_y"], rtol=0, atol=1e-9)
 
 
-def test_oracle2d_matches_reference_at_the_example_size():
-    """The reference example's full size (192 x 384, dt 0.025f, adaptive, correction term
-    evaluated): six frames of the oracle hash to the reference's own arrays, every field of every
-    frame, with the same CFL sub-steps."""
+@pytest.mark.parametrize("name", ["ref2d_eval_a192_hashes", "ref2d_stock_n192_hashes"])
+def test_oracle2d_matches_reference_at_the_example_size(name):
+    """The reference example's full size (192 x 384, dt 0.025f): six frames of the oracle hash to
+    the reference's own arrays, every field of every frame, with the same CFL sub-steps -- adaptive
+    with the correction term evaluated, and the stock reference without adaptivity."""
     import json
     import os as _os
     import sys as _sys
@@ -158,7 +159,7 @@ def test_oracle2d_matches_reference_at_the_example_size():
     _sys.path.insert(0, GOLDEN)
     import make_golden
 
-    rec = json.load(open(_os.path.join(GOLDEN, "ref2d_eval_a192_hashes.json")))
+    rec = json.load(open(_os.path.join(GOLDEN, name + ".json")))
     nx, ny, frames, adaptive = rec["case"]
     o = orc.Oracle2D(nx, ny, adaptive=bool(adaptive))
     subs = []
