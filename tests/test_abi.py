@@ -64,3 +64,19 @@ def test_default_params_match_the_benchmark_scene():
     assert (p.buoy_density, p.buoy_temp, p.decay) == (-0.1, 1.0, 1.0)
     assert (p.src_x, p.src_y, p.src_z, p.src_r) == (0.5, 0.5, 0.12, 0.06)
     assert p.closed_mask == 0b101111  # z+ open
+
+
+@pytest.mark.parametrize("header", ["astg.h", "astg2d.h"])
+def test_headers_compile_as_c99(tmp_path, header):
+    """The boundary is plain C: each header compiles on its own as C99 with -pedantic."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "h.c"
+    src.write_text(f'#include "{header}"\nint main(void) {{ return 0; }}\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        "-c", str(src), "-o", str(tmp_path / "h.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
