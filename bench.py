@@ -31,7 +31,7 @@ for _p in (ROOT, PKG):
         sys.path.insert(0, _p)
 
 COARSEST, LEVELS, DT = 64, 3, 0.01
-WORKLOAD = "octree smoke step, 64^3 coarsest x 3 levels (256^3-equivalent), FP64 MIC(0)-PCG to rel. residual 1e-6"
+WORKLOAD = "octree smoke step, 64^3 coarsest x 3 levels (256^3-eq.), FP64 MIC(0)-PCG to rel. res. 1e-6"
 METRIC = "smoke steps/s"
 
 
@@ -170,7 +170,8 @@ def cpu_baseline_sample(steps):
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": steps / el, "unit": "steps/s", "cores": threads, "kind": "port",
             "sample": f"{steps} steps of the same scene from t=0 (oracle/smoke_oracle.cpp, OpenMP, "
-                      f"bit-identical to the reference's CPU algorithm), {el:.1f} s"}
+                      f"bit-identical to the reference's CPU algorithm), {el:.1f} s",
+            "sample_short": f"{steps} steps from t=0, OpenMP oracle port, {el:.1f} s"}
 
 
 def isolated_solves(args, device):
@@ -590,7 +591,7 @@ def run_ours(args):
     if rank == 0 and args.frames2d > 0:
         flat2d = uniform2d(args, local)
 
-    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+    full = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "coarsest": COARSEST, "levels": LEVELS, "dt": DT,
@@ -604,9 +605,90 @@ def run_ours(args):
     s.close()
     D.barrier()
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        emit(full, args.detail_out)
     D.close()
     return 0
+
+
+LINE_LIMIT = 1400  # characters of the printed line: harnesses that keep only the tail of stdout must see all of it
+
+
+def _r(x, sig=5):
+    """A float rounded to `sig` significant digits (the printed line stays short); other values as given."""
+    if isinstance(x, float):
+        return float(f"{x:.{sig}g}")
+    return x
+
+
+def _pick(d, keys, sig=5):
+    return None if d is None else {k: _r(d.get(k), sig) for k in keys if k in d}
+
+
+def compact_line(full, detail_path):
+    """The one printed JSON line: the contract's keys first (value, unit, config, roofline, cpu_baseline,
+    e2e, clocks, gpu_launches), then one-number summaries of the other sections.  Everything else of
+    `full` (per-kernel times, per-step series of the FP64/mixed comparison, the adjoint and 2-D
+    sections in full) goes to the side file `detail_path`."""
+    cfg = full["config"]
+    line = {k: _r(full[k]) for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                                     "higher_is_better", "scaling", "vs_baseline", "dtype", "data")}
+    line["config"] = {"workload": cfg["workload"], "coarsest": cfg["coarsest"], "levels": cfg["levels"],
+                      "dt": cfg["dt"], "dofs": _r(cfg["dofs_mean"], 6), "l2": "state>L2", "parallelism": cfg["parallelism"]}
+    line["roofline"] = _pick(full["roofline"], ("bound", "kernel", "achieved", "peak", "unit", "frac", "traffic"), 4)
+    line["roofline"]["alg_bytes"] = _r(full["roofline"]["algorithmic_bytes_per_launch"], 4)
+    cb = full.get("cpu_baseline")
+    line["cpu_baseline"] = None if cb is None else {"value": _r(cb["value"]), "unit": cb["unit"], "cores": cb["cores"],
+                                                    "kind": cb["kind"], "sample": cb.get("sample_short", cb["sample"])}
+    line["e2e"] = _pick(full["e2e"], ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"))
+    line["clocks"] = _pick(full["clocks"], ("sm_mhz", "sm_max_mhz", "reasons"))
+    line["gpu_launches"] = full["gpu_launches"]
+    line["pcg_ms_per_solve"] = _r(full["pcg_ms_per_solve"], 4)
+    line["pcg_iters"] = _r(full["pcg_iters_mean"], 4)
+    m = full.get("mixed")
+    if m:
+        line["mixed"] = {"value": _r(m["value"]), "ms_per_step": _r(m["ms_per_step"], 4),
+                         "pcg_ms_per_solve": _r(m["pcg_ms_per_solve"], 4), "converged": m["all_converged"]}
+    adv = full.get("advection")
+    if adv:
+        line["advection_ms"] = _r(adv["ms_per_step"], 4)
+    iso = full.get("isolated_solves")
+    if iso:
+        line["solves"] = {"fp64_ms": _r(iso["fp64"]["ms_per_solve"], 4), "mixed_ms": _r(iso["mixed"]["ms_per_solve"], 4),
+                          "fp64_it": _r(iso["fp64"]["iterations_mean"], 4),
+                          "mixed_it": _r(iso["mixed"]["iterations_mean"], 4), "speedup": _r(iso["mixed_speedup"], 3)}
+    adj = full.get("adjoint")
+    if adj:
+        line["adjoint"] = {"ratio": _r(adj["adjoint_fwd_cost_ratio"], 3),
+                           "grad_err_mixed": _r(adj["grad_rel_error_mixed_vs_fp64"], 3),
+                           "peak_gb": _r(adj["peak_device_bytes"] / 1e9, 3)}
+    pc = full.get("precision_comparison")
+    if pc:
+        line["compare"] = {"dens_max": _r(pc["density_rel_l2_mixed_vs_fp64"]["max"], 3),
+                           "res_mixed": _r(pc["rel_residual_mixed"]["max"], 3),
+                           "res_fp64": _r(pc["rel_residual_fp64"]["max"], 3)}
+    u2 = full.get("uniform2d")
+    if u2:
+        line["uniform2d_fps"] = _r(u2["value"], 4)
+    if detail_path:
+        rel = os.path.relpath(os.path.abspath(detail_path), ROOT)
+        line["detail"] = detail_path if rel.startswith("..") else rel
+    return line
+
+
+def emit(full, detail_path):
+    """Writes `full` to the side file and prints the compact contract line as the last line of stdout."""
+    if detail_path:
+        try:
+            os.makedirs(os.path.dirname(os.path.abspath(detail_path)), exist_ok=True)
+            with open(detail_path, "w") as f:
+                json.dump(full, f, indent=1)
+        except OSError as e:
+            print(f"warning: detail file not written ({e})", file=sys.stderr)
+            detail_path = None
+    s = json.dumps(compact_line(full, detail_path), separators=(",", ":"))
+    if len(s) > LINE_LIMIT:
+        print(f"warning: contract line is {len(s)} characters", file=sys.stderr)
+    print(s, flush=True)
 
 
 def main():
@@ -627,6 +709,8 @@ def main():
     ap.add_argument("--warmup2d", type=int, default=10, help="warm-up frames of the uniform 2-D solver")
     ap.add_argument("--cpu-frames2d", type=int, default=2, help="frames of the 2-D oracle CPU sample (0: skip)")
     ap.add_argument("--only-2d", action="store_true", help="run only the uniform 2-D solver section and print it")
+    ap.add_argument("--detail-out", default=os.path.join(ROOT, "_build", "bench_detail.json"),
+                    help="side file for the sections left out of the printed line ('' to skip)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
