@@ -1,17 +1,19 @@
 // Host-side declarations of the kernel launchers (implemented in astg_step.cu and astg_pcg.cu).
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
 #include <vector>
 #include "astg_device.cuh"
 
 namespace astg {
 
-// number of kernels this library has launched (all handles of the process)
-extern long long g_launches;
-#define ASTG_LAUNCH(...)            \
-    do {                            \
-        ++::astg::g_launches;       \
-        __VA_ARGS__;                \
+// number of kernels this library has launched (all handles of the process; calls on several host
+// threads may count at once)
+extern std::atomic<long long> g_launches;
+#define ASTG_LAUNCH(...)                                                       \
+    do {                                                                       \
+        ::astg::g_launches.fetch_add(1, std::memory_order_relaxed);            \
+        __VA_ARGS__;                                                           \
     } while (0)
 
 // optional CUDA-event timing of the PCG's kernels: 0 forward sweep, 1 backward sweep,

@@ -17,6 +17,7 @@
 // ready flags of the rows it reads.  Every wait is bounded; on timeout the kernel records
 // DS_WAIT_TIMEOUT in the device status word and carries on, so a wait can never hang the GPU.
 #include <cooperative_groups.h>
+#include <cuda.h>
 #include <cstdio>
 #include <algorithm>
 #include <cstdlib>
@@ -33,7 +34,7 @@ namespace cg = cooperative_groups;
 
 namespace astg {
 
-long long g_launches = 0;
+std::atomic<long long> g_launches{0};
 
 // event pairs around profiled launches; drained after each host synchronisation.  On a capturing
 // stream the records become event-record nodes of the graph (external records) in a separate set
@@ -125,8 +126,8 @@ struct BatchGraph {
             cudaError_t e = cudaStreamEndCapture(st, &g);
             if (e == cudaSuccess) e = cudaGraphInstantiate(&exec[k], g, 0);
             if (g) cudaGraphDestroy(g);
-            launches[k] = g_launches - l0;
-            g_launches = l0;
+            launches[k] = g_launches.load() - l0;
+            g_launches -= launches[k];  // captured, not launched: counted at each replay
             if (e != cudaSuccess) {
                 cudaGetLastError();
                 exec[k] = nullptr;
@@ -274,9 +275,18 @@ __global__ void k_amb_levels(LevelSpans sp, const double* parts, double* amb) {
     if (threadIdx.x == 0) *amb = total / (double)count;
 }
 
-// Address of g_amb_scratch on the current device, looked up on the first call made with each
-// device current and kept; the lookup may load this library's device code on that device.
+// Address of g_amb_scratch in the current context, looked up on the first call made with each
+// device current and kept with the context it belongs to; the lookup may load this library's device
+// code on that device.  A context that is destroyed and created again (cudaDeviceReset, or a
+// primary context released by every user and retained anew) reloads the module, possibly at another
+// address, so the cached address is only used while the current context is the one it was taken
+// in; otherwise it is looked up again.  The context handle comes from the driver's cuCtxGetCurrent,
+// reached through the runtime's entry-point query, so this library links no driver library.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
 static std::mutex g_amb_scratch_mu;
+static CtxGetCurrentFn g_ctx_get_current = nullptr;
+static bool g_ctx_query_done = false;
+static CUcontext g_amb_scratch_ctx[NOALLOC_MAX_DEVICES];
 static double* g_amb_scratch_ptr[NOALLOC_MAX_DEVICES];
 cudaError_t mean_temperature_scratch(double** out) {
     int dev = 0;
@@ -284,23 +294,47 @@ cudaError_t mean_temperature_scratch(double** out) {
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_amb_scratch_mu);
-    if (!g_amb_scratch_ptr[dev]) {
+    if (!g_ctx_query_done) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+        g_ctx_query_done = true;
+    }
+    // make the device's primary context current (a no-op when it already is), then name it
+    e = cudaFree(nullptr);
+    if (e != cudaSuccess) return e;
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current && g_ctx_get_current(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+    if (!g_amb_scratch_ptr[dev] || !ctx || ctx != g_amb_scratch_ctx[dev]) {
         double* p = nullptr;
         e = cudaGetSymbolAddress((void**)&p, g_amb_scratch);
         if (e != cudaSuccess) return e;
         g_amb_scratch_ptr[dev] = p;
+        g_amb_scratch_ctx[dev] = ctx;
     }
     *out = g_amb_scratch_ptr[dev];
     return cudaSuccess;
 }
+// Each launch's own status is returned (cudaLaunchKernel), so an error that another call on this
+// host thread left pending is neither reported as this call's nor cleared.
 cudaError_t launch_mean_temperature_static(const double* heat, const LevelSpans& sp, double* amb, cudaStream_t st) {
     double* parts = nullptr;
     cudaError_t e = mean_temperature_scratch(&parts);
     if (e != cudaSuccess) return e;
     int m = sp.partOff[sp.L];
-    if (m > 0) ASTG_LAUNCH(k_tree_sum_levels<<<m, RED_LANES, 0, st>>>(heat, sp, parts));
-    ASTG_LAUNCH(k_amb_levels<<<1, RED_LANES, 0, st>>>(sp, parts, amb));
-    return cudaGetLastError();
+    LevelSpans spv = sp;
+    if (m > 0) {
+        void* args[] = {(void*)&heat, (void*)&spv, (void*)&parts};
+        ++g_launches;
+        e = cudaLaunchKernel((const void*)k_tree_sum_levels, dim3(m), dim3(RED_LANES), args, 0, st);
+        if (e != cudaSuccess) return e;
+    }
+    const double* pc = parts;
+    void* args2[] = {(void*)&spv, (void*)&pc, (void*)&amb};
+    ++g_launches;
+    return cudaLaunchKernel((const void*)k_amb_levels, dim3(1), dim3(RED_LANES), args2, 0, st);
 }
 
 // ------------------------------------------------------------------ exclusive scan (int)

@@ -203,7 +203,11 @@ astg_status astg_extrapolate(astg_handle* h, const char* field, const double* sd
  * Nothing in the scratch needs to start at zero: each call writes every partial it reads.
  * The first call with each device current looks up the scratch's address (cudaGetSymbolAddress),
  * which may load this library's device code onto that device; make that first call before any
- * stream capture begins.  All calls on one device share the scratch: calls whose kernels may
+ * stream capture begins.  The address is kept with the context it was taken in: after the
+ * device's context is destroyed and created again (cudaDeviceReset), the next call looks it up
+ * anew, and should again come before any capture.  ASTG_CUDA_ERROR reports only the failure of this
+ * call's own launches; an error another call left pending on the host thread is neither reported
+ * nor cleared.  All calls on one device share the scratch: calls whose kernels may
  * overlap in time (different streams, or host threads without ordering between them) race on it
  * and must be serialised by the caller. */
 astg_status astg_mean_temperature_noalloc(const double* d_heat_oct, const int64_t* level_slots, int levels,
