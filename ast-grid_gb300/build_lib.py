@@ -1,7 +1,9 @@
 """Builds libastgrid_gpu.so in-tree (ast-grid_gb300/_build/) with nvcc for sm_103a.
 
-FMA contraction is off in device and host code so the FP64 step follows the reference's
-IEEE operation order (the mixed-precision kernels are unaffected: they are bandwidth bound)."""
+FMA contraction is off in device and host code so the FP64 step follows the reference's IEEE
+operation order; where the kernels fuse a multiply and an add they say so with an explicit fma().
+The FP32 kernels of the mixed form are built under the same flag; their sweeps are bound by the
+dependency chain (latency), not by arithmetic, so contraction would not change their speed much."""
 import os
 import subprocess
 from concurrent.futures import ThreadPoolExecutor

@@ -1,7 +1,7 @@
 """Regenerate the golden fixtures from the reference solver itself.
 
 Builds the reference's own sources with oracle/ref/Makefile (reference checkout at $ASTG_REF,
-default /root/reference), runs the fixture harness oracle/ref/ref_harness.cpp on small cases
+default: a directory named "reference" beside this repository), runs the fixture harness oracle/ref/ref_harness.cpp on small cases
 of the benchmark scene, and stores the dumps as compressed .npz files next to this script.
 
     python tests/golden/make_golden.py
@@ -226,7 +226,7 @@ def ckpt_fixtures(harness):
 
 
 def main():
-    ref = os.environ.get("ASTG_REF", "/root/reference")
+    ref = os.environ.get("ASTG_REF", os.path.join(os.path.dirname(ROOT), "reference"))
     subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref", "Makefile"), f"REF={ref}",
                            "-j8"])
     harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
