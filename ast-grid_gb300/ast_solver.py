@@ -26,7 +26,7 @@ FP64, MIXED = 0, 1
 
 # exported symbols of include/astg.h
 SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_stage",
-           "astg_set_solver_parameters", "astg_set_precision", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
+           "astg_set_solver_parameters", "astg_set_precision", "astg_set_reduction_order", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
            "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate",
            "astg_restart", "astg_save_checkpoint", "astg_tape_start", "astg_tape_stop", "astg_adjoint_reset",
            "astg_backward", "astg_step_vjp", "astg_stage_vjp", "astg_adjoint_probe", "astg_set_tilt_adaptivity",
@@ -99,6 +99,7 @@ def lib(path=None):
         L.astg_stage.argtypes = [c_p, ctypes.c_int, ctypes.c_double]
         L.astg_set_solver_parameters.argtypes = [c_p, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.astg_set_precision.argtypes = [c_p, ctypes.c_int]
+        L.astg_set_reduction_order.argtypes = [c_p, ctypes.c_int, ctypes.c_int]
         L.astg_set_profiling.argtypes = [c_p, ctypes.c_int]
         L.astg_last_solve.argtypes = [c_p, ctypes.POINTER(SolveStats)]
         L.astg_size.argtypes = [c_p, ctypes.c_int]
@@ -234,6 +235,12 @@ class OctreeSmoke3:
 
     def set_precision(self, prec):
         self._check(lib().astg_set_precision(self._h, {"fp64": FP64, "mixed": MIXED}.get(prec, prec)))
+
+    def set_reduction_order(self, order, workers=8):
+        """"library" (the default: fixed reduction tree, fused sweep updates) or "reference" (the
+        reference's own arithmetic, bit for bit; `workers` is the reference's thread-pool size, on
+        which its BLAS::sum slices depend)."""
+        self._check(lib().astg_set_reduction_order(self._h, {"library": 0, "reference": 1}.get(order, order), workers))
 
     def set_profiling(self, on):
         self._check(lib().astg_set_profiling(self._h, 1 if on else 0))

@@ -88,6 +88,7 @@ struct astg_handle {
     uint8_t* dOpen = nullptr;
     uint8_t* dFixed = nullptr;
     Proj J{};
+    int refWorkers = 8;  // workers of the reference-order mean temperature
     double* dAmb = nullptr;
     double* dParts = nullptr;
     int* dPartOff = nullptr;
@@ -1025,7 +1026,8 @@ struct astg_handle {
                 }
                 break;
             case 1:
-                launch_mean_temperature(d, C.hO, dParts, dPartOff, partOff.data(), dAmb, st);
+                if (J.refOrder) launch_mean_temperature_ref(d, C.hO, refWorkers, dAmb, st);
+                else launch_mean_temperature(d, C.hO, dParts, dPartOff, partOff.data(), dAmb, st);
                 launch_force(d, C, dOpen, dAmb, dt, st);
                 break;
             case 2: launch_walls_and_ghost(d, C, dLastWriter, st); break;
@@ -1769,6 +1771,15 @@ astg_status astg_set_profiling(astg_handle* h, int on) {
 astg_status astg_set_precision(astg_handle* h, astg_precision prec) {
     if (!h || (prec != ASTG_FP64 && prec != ASTG_MIXED)) return ASTG_BAD_ARG;
     h->P.precision = prec;
+    return ASTG_OK;
+}
+
+astg_status astg_set_reduction_order(astg_handle* h, astg_order order, int workers) {
+    if (!h || (order != ASTG_ORDER_LIBRARY && order != ASTG_ORDER_REFERENCE)) return ASTG_BAD_ARG;
+    if (order == ASTG_ORDER_REFERENCE && (workers < 1 || workers > astg::REF_MAX_WORKERS)) return ASTG_BAD_ARG;
+    h->J.refOrder = order == ASTG_ORDER_REFERENCE;
+    h->J.unfused = h->J.refOrder;
+    if (h->J.refOrder) h->refWorkers = workers;
     return ASTG_OK;
 }
 

@@ -42,6 +42,7 @@ struct KProf {
 
 constexpr int ROW_W = 32;   // padded row width during assembly (rows have at most ~21 entries)
 constexpr int PC_MAXE = 8;  // factor entries per row held in the padded records
+constexpr int REF_MAX_WORKERS = 256;  // worker count of the reference-order mean temperature
 
 // scalars of the PCG kept on the device
 enum { SC_RESID0 = 0, SC_TOL, SC_RHO, SC_RESID, SC_ALPHA, SC_BETA, SC_COUNT };
@@ -139,6 +140,10 @@ struct Proj {
     float* z32;
     float* q32;
     size_t pcSmem;   // its dynamic shared memory per CTA in the current solve
+    // reduction order: 0 the library's (fixed tree, fused sweep updates), 1 the reference's (Eigen
+    // dot order, separate multiply and subtract in the sweeps)
+    int refOrder;
+    int unfused;     // sweep updates as a product and a subtraction
     // PCG
     double* x;
     double* r;
@@ -191,6 +196,8 @@ struct LevelSpans {
     int partOff[MAXL + 1];    // first partial of each level
 };
 cudaError_t launch_mean_temperature_static(const double* heat, const LevelSpans& sp, double* amb, cudaStream_t st);
+// the same in the reference's order (BLAS::sum's per-worker slices, `workers` workers)
+void launch_mean_temperature_ref(const Dev& d, const double* hO, int workers, double* amb, cudaStream_t st);
 void launch_force(const Dev& d, const Fields& F, const uint8_t* open, const double* amb, double dt, cudaStream_t st);
 void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);
 void launch_velocity_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);

@@ -12,6 +12,15 @@
 // scarce resource of the sweeps on this part, and the fused form halves it (measured 0.58 ->
 // 0.46 ms per application at the 256^3-equivalent size).
 //
+// Reference order (astg_set_reduction_order, P.refOrder): the same solve in the reference's own
+// arithmetic, for bit-for-bit parity with it: the dot products in Eigen 3.3.7's order (two SSE2
+// packets of two doubles, so four running lanes over groups of four, Eigen/src/Core/Redux.h, as
+// the reference's BLAS::dot calls a.dot(b), include/pcgsolver/blas_wrapper.h:112-115), the sweep
+// updates as a product and a subtraction, and the mean temperature as BLAS::sum's per-worker
+// slice sums added in worker order (blas_wrapper.h:101-110 over ThreadPool::parallelForPlainTF,
+// include/thread_pool.h:319-348).  These are serial chains (n / 4 and n / workers additions):
+// a parity mode, not the fast path.
+//
 // Dependencies between rows (factorisation, both sweeps) are resolved without global barriers:
 // rows are handed out in dependency order from an atomic counter and each row waits on per-row
 // ready flags of the rows it reads.  Every wait is bounded; on timeout the kernel records
@@ -155,7 +164,18 @@ static int log2_exact(int v) {
     return lg;
 }
 constexpr int RED_LANES = 256, RED_PER_LANE = 8, RED_CHUNK = RED_LANES * RED_PER_LANE;
-constexpr long long SPIN_LIMIT = 1LL << 24;  // ~seconds at nanosleep(64): far above any real wait
+constexpr long long SPIN_LIMIT = 1LL << 24;
+// One update z_i -= L_ij z_j of a MIC(0) sweep: the library's order is one fused multiply-subtract;
+// the reference's order (P.unfused) is a product, then a subtraction, as its column loops
+// (include/pcgsolver/pcg_solver.h:211-253) compute it.
+template <typename T>
+__device__ __forceinline__ T sweep_update(bool unfused, T acc, T v, T zk) {
+    if (unfused) {
+        T prod = v * zk;
+        return acc - prod;
+    }
+    return fma(-v, zk, acc);
+}  // ~seconds at nanosleep(64): far above any real wait
 
 // ------------------------------------------------------------------ fixed-tree reduction
 __device__ inline double block_tree(double v, double* sh) {
@@ -206,6 +226,118 @@ __device__ inline double fold_partials(const double* part, long long m, double* 
         if (i < m) acc = acc + part[i];
     }
     return block_tree(acc, sh);
+}
+
+// ------------------------------------------------------------------ reference-order reductions
+// Eigen's dot of a and b (no fused multiply-add): lanes l_k, k = 0..3, start at a[k] b[k] and add
+// a[i] b[i] for i = k + 4, k + 8, ... below the largest multiple of four; then l0 + l2 and l1 + l3,
+// one more pair when n mod 4 >= 2, their sum, and the scalar tail.  The result goes to part[0] and
+// part[1 .. chunks) are zeroed, so the fixed-tree fold of the partials that follows returns it
+// unchanged (adding zeros is exact).  One block of 32 threads.
+__global__ void k_dot_ref(const double* a, const double* b, const int* nptr, double* part) {
+    __shared__ double lane[4];
+    const long long n = *nptr;
+    const long long asz2 = (n / 4) * 4, asz = (n / 2) * 2;
+    const int t = threadIdx.x;
+    if (asz > 2 && t < 4) {
+        double l = a[t] * b[t];
+#pragma unroll 8
+        for (long long i = 4 + t; i < asz2; i += 4) {
+            double prod = a[i] * b[i];
+            l = l + prod;
+        }
+        lane[t] = l;
+    }
+    __syncthreads();
+    if (t == 0) {
+        double r;
+        if (asz == 0) {
+            r = 0.0;
+            for (long long i = 0; i < n; ++i) {
+                double prod = a[i] * b[i];
+                r = r + prod;
+            }
+        } else {
+            double l0, l1;
+            if (asz > 2) {
+                l0 = lane[0] + lane[2];
+                l1 = lane[1] + lane[3];
+                if (asz > asz2) {
+                    double p0 = a[asz2] * b[asz2], p1 = a[asz2 + 1] * b[asz2 + 1];
+                    l0 = l0 + p0;
+                    l1 = l1 + p1;
+                }
+            } else {
+                l0 = a[0] * b[0];
+                l1 = a[1] * b[1];
+            }
+            r = l0 + l1;
+            for (long long i = asz; i < n; ++i) {
+                double prod = a[i] * b[i];
+                r = r + prod;
+            }
+        }
+        part[0] = r;
+    }
+    const long long chunks = (n + RED_CHUNK - 1) / RED_CHUNK;
+    for (long long c = 1 + t; c < chunks; c += blockDim.x) part[c] = 0.0;
+}
+void launch_dot_ref(const double* a, const double* b, const int* nptr, double* part, cudaStream_t st) {
+    ASTG_LAUNCH(k_dot_ref<<<1, 32, 0, st>>>(a, b, nptr, part));
+}
+// BLAS::sum over [0, size) with `workers` workers: slice = round((size + 1) / workers) (at least 1,
+// the reference counts end - start + 1), worker i < workers - 1 sums [i slice, (i + 1) slice) while
+// slices remain, the last running worker takes the rest; each slice from 0.0 in index order, the
+// slice sums added from 0.0 in worker order
+__device__ double ref_sum(const double* v, long long size, int workers, double* sums, long long* lo, long long* hi) {
+    const int t = threadIdx.x;
+    if (t == 0) {
+        long long slice = llround((double)(size + 1) / (double)workers);
+        if (slice < 1) slice = 1;
+        long long i1 = 0, i2 = min(slice, size);
+        int i = 0;
+        for (int w = 0; w < workers; ++w) lo[w] = hi[w] = 0;
+        for (; i + 1 < workers && i1 < size; ++i) {
+            lo[i] = i1;
+            hi[i] = i2;
+            i1 = i2;
+            i2 = min(i2 + slice, size);
+        }
+        if (i1 < size) {
+            lo[i] = i1;
+            hi[i] = size;
+        }
+    }
+    __syncthreads();
+    for (int w = t; w < workers; w += blockDim.x) {
+        double x = 0.0;
+        for (long long k = lo[w]; k < hi[w]; ++k) x = x + v[k];
+        sums[w] = x;
+    }
+    __syncthreads();
+    double acc = 0.0;
+    if (t == 0)
+        for (int w = 0; w < workers; ++w) acc = acc + sums[w];
+    __syncthreads();
+    return acc;
+}
+// addForce's ambT in the reference's order (src/octree_omnigrid_solver3.cpp:922-929 with
+// BLAS::sum per level); one block
+__global__ void k_amb_ref(Dev d, const double* hO, int workers, double* amb) {
+    __shared__ double sums[REF_MAX_WORKERS];
+    __shared__ long long lo[REF_MAX_WORKERS], hi[REF_MAX_WORKERS];
+    double total = 0.0;
+    long long count = 0;
+    for (int l = 0; l < d.L; ++l) {
+        long long nl = d.lN[l] + d.lG[l];
+        double s = ref_sum(hO + d.loff[l], nl, workers, sums, lo, hi);
+        total += s * (l == 0 ? 1 : 8);
+        count += nl * (l == 0 ? 1 : 8);
+    }
+    if (threadIdx.x == 0) *amb = total / (double)count;
+}
+void launch_mean_temperature_ref(const Dev& d, const double* hO, int workers, double* amb, cudaStream_t st) {
+    ASTG_LAUNCH(k_amb_ref<<<1, REF_MAX_WORKERS, 0, st>>>(d, hO, workers, amb));
 }
 
 // ------------------------------------------------------------------ mean temperature
@@ -901,7 +1033,7 @@ __global__ void k_sweep_fwd_cluster(Proj P, const double* r, double* z) {
         for (int p = P.levelPtr[g] + t; p < p1; p += nth) {
             int i = P.perm[p];
             double acc = r[i];
-            for (int q = P.fptr[p]; q < P.fptr[p + 1]; ++q) acc = fma(-P.fval[q], __ldcg(z + P.fcol[q]), acc);
+            for (int q = P.fptr[p]; q < P.fptr[p + 1]; ++q) acc = sweep_update(P.unfused != 0, acc, P.fval[q], __ldcg(z + P.fcol[q]));
             z[i] = acc * P.invdiag[i];
         }
         cl.sync();
@@ -919,7 +1051,7 @@ __global__ void k_sweep_bwd_cluster(Proj P, const double* unused, double* z) {
         for (int p = P.levelPtr[g] + t; p < p1; p += nth) {
             int i = P.perm[p];
             double acc = __ldcg(z + i);
-            for (int q = P.bptr[p]; q < P.bptr[p + 1]; ++q) acc = fma(-P.bval[q], __ldcg(z + P.bcol[q]), acc);
+            for (int q = P.bptr[p]; q < P.bptr[p + 1]; ++q) acc = sweep_update(P.unfused != 0, acc, P.bval[q], __ldcg(z + P.bcol[q]));
             z[i] = acc * P.invdiag[i];
         }
         cl.sync();
@@ -976,14 +1108,14 @@ __device__ __forceinline__ void pc_row(const Proj& P, const PcRow& w, bool fwd, 
     double acc = fwd ? w.rhs : ld_ds(ai);
 #pragma unroll
     for (int e = 0; e < PC_MAXE; ++e)
-        if (e < w.cnt) acc = fma(-w.val[e], zk[e], acc);
+        if (e < w.cnt) acc = sweep_update(P.unfused != 0, acc, w.val[e], zk[e]);
     if (w.cnt > PC_MAXE) {  // rows longer than the padded record: the rest from the compact arrays
         const int* cc = fwd ? P.fcol : P.bcol;
         const double* vv = fwd ? P.fval : P.bval;
         int q0 = (fwd ? P.fptr : P.bptr)[w.p];
         for (int e = PC_MAXE; e < w.cnt; ++e) {
             int k = cc[q0 + e];
-            acc = fma(-vv[q0 + e], ld_ds(rb[k & msk] + (uint32_t)(k >> lg) * 8u), acc);
+            acc = sweep_update(P.unfused != 0, acc, vv[q0 + e], ld_ds(rb[k & msk] + (uint32_t)(k >> lg) * 8u));
         }
     }
     st_ds(ai, acc * w.invd);
@@ -1156,7 +1288,7 @@ template <typename T>
 __device__ __forceinline__ const T* pca_gptr(T* const* win, int packed) {
     return win[packed >> 24] + (packed & 0xffffff);
 }
-template <typename T>
+template <typename T, bool UNFUSED>
 __device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaData<T>& D, const PcaRow<T>& w, bool fwd,
                                               uint32_t own, T* const* win, int* status) {
     typedef Pca<T> K;
@@ -1199,7 +1331,7 @@ __device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaData<T>& D
 #pragma unroll
                     for (int e = 0; e < PCA_MAXE; ++e) {
                         if (e >= lim) break;
-                        acc = fma(-val[e], K::val(v[e]), acc);
+                        acc = sweep_update(UNFUSED, acc, val[e], K::val(v[e]));
                     }
                     part = true;
                 }
@@ -1208,7 +1340,7 @@ __device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaData<T>& D
             while (part && got < w.cnt) {
                 Bits x = K::ld(pca_gptr(win, oc[q0 + got]));
                 if (x == K::EMPTY) break;
-                acc = fma(-ov[q0 + got], K::val(x), acc);
+                acc = sweep_update(UNFUSED, acc, ov[q0 + got], K::val(x));
                 ++got;
             }
             if (part && got >= w.cnt) {
@@ -1226,7 +1358,7 @@ __device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaData<T>& D
         }
     }
 }
-template <typename T>
+template <typename T, bool UNFUSED>
 __global__ void __launch_bounds__(PCA_THREADS, 1) k_precond_async(Proj P, PcaData<T> D, T* z, int* status, int lgCS) {
     typedef Pca<T> K;
     if (*P.done) return;
@@ -1262,7 +1394,7 @@ __global__ void __launch_bounds__(PCA_THREADS, 1) k_precond_async(Proj P, PcaDat
         pca_load(P, D, base, pick(0), rows, fwd, W);
         for (int k = 0; k < rounds; ++k) {
             pca_load(P, D, base, pick(k + 1), rows, fwd, X);
-            pca_solve_row(P, D, W, fwd, own, win, status);
+            pca_solve_row<T, UNFUSED>(P, D, W, fwd, own, win, status);
             W = X;
         }
         cl.sync();  // sweep finished everywhere (global and shared writes ordered at cluster scope)
@@ -1310,7 +1442,8 @@ static cudaError_t launch_precond_async(const Dev& d, const Proj& P, const PcaDa
     cfg.attrs = at;
     cfg.numAttrs = 1;
     ++g_launches;
-    return cudaLaunchKernelEx(&cfg, k_precond_async<T>, P, D, z, d.status, log2_exact(P.pcCluster));
+    if (P.unfused) return cudaLaunchKernelEx(&cfg, k_precond_async<T, true>, P, D, z, d.status, log2_exact(P.pcCluster));
+    return cudaLaunchKernelEx(&cfg, k_precond_async<T, false>, P, D, z, d.status, log2_exact(P.pcCluster));
 }
 static PcaData<double> pca_data64(const Proj& P) {
     return PcaData<double>{P.fvalP, P.bvalP, P.linvd, P.rl, P.yl, P.fval, P.bval};
@@ -1320,7 +1453,7 @@ static PcaData<double> pca_data64(const Proj& P) {
 // Each solve then uses ceil(n / CS) doubles per CTA and falls back to the global-memory sweeps
 // when they do not fit.
 int choose_dsmem_cluster(bool async, size_t* smemMax) {
-    const void* kern = async ? (const void*)k_precond_async<double> : (const void*)k_precond_dsmem;
+    const void* kern = async ? (const void*)k_precond_async<double, false> : (const void*)k_precond_dsmem;
     const int threads = async ? PCA_THREADS : PC_THREADS;
     *smemMax = 0;
     cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -1340,11 +1473,16 @@ int choose_dsmem_cluster(bool async, size_t* smemMax) {
         return 0;
     }
     if (async) {  // the FP32 instance of the mixed-precision solve: same launch shape
-        const void* k32 = (const void*)k_precond_async<float>;
-        cudaFuncSetAttribute(k32, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        if (cudaFuncSetAttribute(k32, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
-            cudaGetLastError();
-            return 0;
+        // the other instances (FP32 of the mixed-precision solve; the reference order's separate
+        // multiply and subtract): same launch shape
+        const void* others[3] = {(const void*)k_precond_async<float, false>, (const void*)k_precond_async<float, true>,
+                                 (const void*)k_precond_async<double, true>};
+        for (const void* k2 : others) {
+            cudaFuncSetAttribute(k2, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            if (cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+                cudaGetLastError();
+                return 0;
+            }
         }
     }
     for (int cs : {16, 8}) {
@@ -1553,7 +1691,7 @@ __global__ void k_sweep_fwd(Dev d, Proj P, const double* r, double* z, int epoch
             int k = P.col[q];
             if (k >= i) break;
             wait_flag(d, P.ready + k, epoch);
-            acc = fma(-P.Lv[P.tpos[q]], z[k], acc);
+            acc = sweep_update(P.unfused != 0, acc, P.Lv[P.tpos[q]], z[k]);
         }
         z[i] = acc * P.invdiag[i];
         __threadfence();
@@ -1574,7 +1712,7 @@ __global__ void k_sweep_bwd(Dev d, Proj P, double* z, int epoch) {
             int c = P.col[q];
             if (c <= i) continue;
             wait_flag(d, P.ready + c, epoch);
-            acc = fma(-P.Lv[q], z[c], acc);
+            acc = sweep_update(P.unfused != 0, acc, P.Lv[q], z[c]);
         }
         z[i] = acc * P.invdiag[i];
         __threadfence();
@@ -1954,7 +2092,8 @@ int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& e
     if (P.pcActive) ASTG_LAUNCH(k_to_level_order<<<nblk(maxRows), TB, 0, st>>>(P, r));
     if (P.wave) ASTG_LAUNCH(k_to_wave_order<<<nblk(maxRows), TB, 0, st>>>(P, r));
     precond(d, P, r, z, epoch, st, prof);
-    ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
+    if (P.refOrder) launch_dot_ref(z, r, P.nDof, P.part, st);
+    else ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
     ASTG_LAUNCH(k_pcg_start<<<1, RED_LANES, 0, st>>>(P, P.part, tolFactor));
     ASTG_LAUNCH(k_copy<<<nblk(maxRows), TB, 0, st>>>(z, s, P.nDof));
     int launched = 0;
@@ -1964,11 +2103,13 @@ int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& e
             prof_begin(pf, 2, st);
             ASTG_LAUNCH(k_spmv_dot<<<chunks, SPMV_THREADS, 0, st>>>(P, s, z, P.part));
             prof_end(pf, st);
+            if (P.refOrder) launch_dot_ref(s, z, P.nDof, P.part, st);
             ASTG_LAUNCH(k_alpha<<<1, RED_LANES, 0, st>>>(P, P.part));
             ASTG_LAUNCH(k_update_xr<<<nblk(maxRows), TB, 0, st>>>(P, x, r, s, z));
             ASTG_LAUNCH(k_check<<<1, 1, 0, st>>>(P, maxIter));
             precond(d, P, r, z, epoch, st, pf);
-            ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
+            if (P.refOrder) launch_dot_ref(z, r, P.nDof, P.part, st);
+            else ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
             ASTG_LAUNCH(k_beta<<<1, RED_LANES, 0, st>>>(P, P.part));
             ASTG_LAUNCH(k_update_s<<<nblk(maxRows), TB, 0, st>>>(P, s, z));
         }

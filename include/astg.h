@@ -104,6 +104,23 @@ astg_status astg_stage(astg_handle* h, int stage, double dt);
 astg_status astg_set_solver_parameters(astg_handle* h, double tol, int max_iter, double omega, double min_diag);
 astg_status astg_set_precision(astg_handle* h, astg_precision prec);
 
+/* Order of the floating-point reductions of the FP64 solve and of addForce's mean temperature.
+ * ASTG_ORDER_LIBRARY (the default, the fast path): one fixed reduction tree for every dot product
+ * and sum, each sweep update one fused multiply-subtract; results are reproducible, and match the
+ * reference to the PCG tolerance.  ASTG_ORDER_REFERENCE: the reference's own arithmetic, so the
+ * solve reproduces it bit for bit: dot products in Eigen 3.3.7's SSE2 order (BLAS::dot,
+ * include/pcgsolver/blas_wrapper.h:112-115), the MIC(0) sweep updates as a multiply and a
+ * subtraction (include/pcgsolver/pcg_solver.h:211-253), and the mean temperature as BLAS::sum's
+ * per-worker slice sums (blas_wrapper.h:101-110, include/thread_pool.h:319-348) over `workers`
+ * workers, the reference's thread-pool size (its hardware concurrency: the slices depend on it),
+ * 1..256.  The reference order runs the dot products and sums as serial chains: it is a parity
+ * mode, much slower than the library order.  It applies to the FP64 form (ASTG_FP64). */
+typedef enum astg_order {
+    ASTG_ORDER_LIBRARY = 0,
+    ASTG_ORDER_REFERENCE = 1
+} astg_order;
+astg_status astg_set_reduction_order(astg_handle* h, astg_order order, int workers);
+
 /* CUDA-event timing of the PCG's main kernels (forward and backward MIC(0) sweeps, SpMV + dot,
  * factorisation), read back as astg_get(h, "kernel_ms", ...).  No counterpart in the reference:
  * it replaces the BENCHMARK_SCOPED_TIMER_SECTION probes (include/global_benchmark.h:33-43). */
