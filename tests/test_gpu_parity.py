@@ -189,12 +189,13 @@ def test_config0_fifty_steps_bit_identical_to_oracle():
 
 def test_mixed_form_tracks_fp64_oracle():
     """The mixed-precision form against the FP64 oracle over 20 steps (16^3 coarsest, 3 levels):
-    per step the density within 1e-5 and the pressure within 1e-4 relative (L2), and the solve's
-    true FP64 residual at most 1e-6 |b|_inf."""
+    per step the density and the pressure within 1e-5 relative (L2), and the solve's true FP64
+    residual at most 1e-6 |b|_inf."""
     import numpy as np
 
     s = solver(16, 3, precision="mixed")
     o = oracle(16, 3)
+    worst_d = worst_p = 0.0
     for k in range(20):
         s.update(DT)
         o.step(DT)
@@ -202,8 +203,10 @@ def test_mixed_form_tracks_fp64_oracle():
         assert st.converged == 1 and st.outer >= 1
         assert st.residual <= st.tolerance
         a, b = o.get("density_oct"), s.get("density_oct")
-        assert np.linalg.norm(b - a) <= 1e-5 * np.linalg.norm(a), k
+        worst_d = max(worst_d, np.linalg.norm(b - a) / np.linalg.norm(a))
         pa, pb = o.get("p"), s.get("p")
-        if len(pa) == len(pb):
-            assert np.linalg.norm(pb - pa) <= 1e-4 * np.linalg.norm(pa), k
+        assert len(pa) == len(pb), k  # same DOF map: no tilt decision differs
+        worst_p = max(worst_p, np.linalg.norm(pb - pa) / np.linalg.norm(pa))
+    print(f"mixed vs FP64 over 20 steps: density {worst_d:.2e}, pressure {worst_p:.2e}")
+    assert worst_d <= 1e-5 and worst_p <= 1e-5
     s.close()

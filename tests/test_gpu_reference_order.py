@@ -89,14 +89,16 @@ def test_standalone_solve_reproduces_reference_iterates(name):
     s.close()
 
 
-def test_config0_fifty_steps_hash_identical_to_reference():
+@pytest.mark.parametrize("name", ["ref_c32_l3_hashes", "ref_c64_l3_hashes"])
+def test_full_size_hash_identical_to_reference(name):
     """The reference's CPU-runnable configuration (32^3 coarsest x 3 levels, 128^3-equivalent) for its
-    full 50 steps: after every step the sha256 of every state array, the tilt layout, the DOF maps,
-    the pressure and the iteration count equal the reference's own."""
+    full 50 steps, and the benchmark size (64^3 x 3 levels, 256^3-equivalent) for 20 steps: after
+    every step the sha256 of every state array, the tilt layout, the DOF maps, the pressure and the
+    iteration count equal the reference's own."""
     sys.path.insert(0, GOLDEN)
     import make_golden
 
-    rec = json.load(open(os.path.join(GOLDEN, "ref_c32_l3_hashes.json")))
+    rec = json.load(open(os.path.join(GOLDEN, name + ".json")))
     c, lv, steps = rec["case"]
     s = solver(c, lv)
     get = getter(s)
