@@ -25,7 +25,8 @@ STATUS = {0: "ok", 1: "bad argument", 2: "CUDA error", 3: "not converged", 4: "d
 FP64, MIXED = 0, 1
 
 # exported symbols of include/astg.h
-SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_stage",
+SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_update",
+           "astg_set_max_cfl", "astg_cfl", "astg_stage",
            "astg_set_solver_parameters", "astg_set_precision", "astg_set_reduction_order", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
            "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate",
            "astg_restart", "astg_save_checkpoint", "astg_tape_start", "astg_tape_stop", "astg_adjoint_reset",
@@ -99,6 +100,9 @@ def lib(path=None):
         L.astg_stage.argtypes = [c_p, ctypes.c_int, ctypes.c_double]
         L.astg_set_solver_parameters.argtypes = [c_p, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.astg_set_precision.argtypes = [c_p, ctypes.c_int]
+        L.astg_update.argtypes = [c_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(StepStats)]
+        L.astg_set_max_cfl.argtypes = [c_p, ctypes.c_double]
+        L.astg_cfl.argtypes = [c_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.astg_set_reduction_order.argtypes = [c_p, ctypes.c_int, ctypes.c_int]
         L.astg_set_profiling.argtypes = [c_p, ctypes.c_int]
         L.astg_last_solve.argtypes = [c_p, ctypes.POINTER(SolveStats)]
@@ -224,8 +228,34 @@ class OctreeSmoke3:
             raise AstgError(st, lib().astg_last_error(self._h).decode())
         return st
 
+    # Solver::useFixedTimeStep (include/solver.h:21).  The reference defaults to false (CFL sub-steps);
+    # these handles default to the benchmark scene's fixed step.
+    useFixedTimeStep = True
+
     def update(self, dt):
-        return self._check(lib().astg_step(self._h, dt, ctypes.byref(self.last_step)), allow=(ASTG_NOT_CONVERGED,))
+        """Solver::update(dt): one fixed step, or (useFixedTimeStep False) CFL sub-steps whose count
+        is left in self.last_substeps."""
+        if self.useFixedTimeStep:
+            self.last_substeps = 1
+            return self._check(lib().astg_step(self._h, dt, ctypes.byref(self.last_step)), allow=(ASTG_NOT_CONVERGED,))
+        n = ctypes.c_int(0)
+        st = self._check(lib().astg_update(self._h, dt, ctypes.byref(n), ctypes.byref(self.last_step)),
+                         allow=(ASTG_NOT_CONVERGED,))
+        self.last_substeps = n.value
+        return st
+
+    def setMaxCfl(self, cfl):
+        self._check(lib().astg_set_max_cfl(self._h, cfl))
+
+    def cfl(self, dt):
+        c = ctypes.c_int(0)
+        self._check(lib().astg_cfl(self._h, dt, ctypes.byref(c), None))
+        return c.value
+
+    def numberOfSubTimeSteps(self, dt):
+        k = ctypes.c_int(0)
+        self._check(lib().astg_cfl(self._h, dt, None, ctypes.byref(k)))
+        return k.value
 
     def stage(self, i, dt):
         self._check(lib().astg_stage(self._h, i, dt))

@@ -5,6 +5,7 @@
 // PCG's stopping test and the status word, reads a few bytes back.
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -1076,6 +1077,59 @@ struct astg_handle {
         }
     }
 
+    // ---------------------------------------------------------------- adaptive update
+    // Solver::update's adaptive branch (src/solver.cpp:21-41, useFixedTimeStep = false) with
+    // numberOfSubTimeSteps / cfl (src/octree_omnigrid_solver3.cpp:1060-1122)
+    double maxCfl = 3.0;  // the reference's default (include/octree_omnigrid_solver3.h:84)
+    bool updateConverged = true;  // every sub-step's solve of the last update converged
+    unsigned long long* dMaxV = nullptr;
+    double maxFace() {
+        if (!dMaxV) dMaxV = dalloc<unsigned long long>(1);
+        ck(cudaMemsetAsync(dMaxV, 0, sizeof(unsigned long long), st), "memset");
+        launch_max_face(d, F[cur].mac, dMaxV, st);
+        unsigned long long bits = 0;
+        ck(cudaMemcpyAsync(&bits, dMaxV, sizeof bits, cudaMemcpyDeviceToHost, st), "max velocity");
+        ck(cudaStreamSynchronize(st), "sync");
+        double v;
+        memcpy(&v, &bits, sizeof v);
+        return v;
+    }
+    // cfl(dt): dt * maxV / delta_h (delta_h = the finest spacing), truncated to int as the reference
+    // returns it
+    int cfl(double dt) { return (int)(dt * maxFace() / dx); }
+    int numberOfSubTimeSteps(double dt) {
+        int k = (int)std::ceil(cfl(dt) / maxCfl);
+        return k > 1 ? k : 1;
+    }
+    // sub-steps of remaining / k while more than EPSILON remains, k recomputed from the current
+    // velocity before each; the statistics are the last sub-step's, with the times summed
+    void update(double dt, int* substeps, astg_step_stats* out) {
+        double remaining = dt;
+        int n = 0;
+        astg_step_stats one{}, sum{};
+        updateConverged = true;
+        while (remaining > std::numeric_limits<double>::epsilon()) {
+            int k = numberOfSubTimeSteps(remaining);
+            double actual = remaining / (double)k;
+            step(actual, &one);
+            if (last.converged == 0) updateConverged = false;
+            sum.ms_total += one.ms_total;
+            sum.ms_force += one.ms_force;
+            sum.ms_project += one.ms_project;
+            sum.ms_advect += one.ms_advect;
+            remaining -= actual;
+            ++n;
+        }
+        if (substeps) *substeps = n;
+        if (out) {
+            *out = one;
+            out->ms_total = sum.ms_total;
+            out->ms_force = sum.ms_force;
+            out->ms_project = sum.ms_project;
+            out->ms_advect = sum.ms_advect;
+        }
+    }
+
     // ---------------------------------------------------------------- adjoint
     // Reverse mode of astg_step with the topology frozen (tilt adaptivity off).  The cotangent of
     // the state lives in GA[ga] (Fields layout; te / tf point at the frozen forward arrays), the
@@ -1772,6 +1826,31 @@ astg_status astg_set_precision(astg_handle* h, astg_precision prec) {
     if (!h || (prec != ASTG_FP64 && prec != ASTG_MIXED)) return ASTG_BAD_ARG;
     h->P.precision = prec;
     return ASTG_OK;
+}
+
+astg_status astg_update(astg_handle* h, double dt, int* substeps, astg_step_stats* stats) {
+    if (!h || !(dt >= 0)) return ASTG_BAD_ARG;
+    astg_status s = guard(h, [&] { h->update(dt, substeps, stats); });
+    if (s == ASTG_OK && !h->updateConverged) return ASTG_NOT_CONVERGED;
+    return s;
+}
+
+astg_status astg_set_max_cfl(astg_handle* h, double max_cfl) {
+    if (!h || !(max_cfl > 0)) return ASTG_BAD_ARG;
+    h->maxCfl = max_cfl;
+    return ASTG_OK;
+}
+
+astg_status astg_cfl(astg_handle* h, double dt, int* cfl, int* substeps) {
+    if (!h || !(dt >= 0)) return ASTG_BAD_ARG;
+    return guard(h, [&] {
+        int c = h->cfl(dt);
+        if (cfl) *cfl = c;
+        if (substeps) {
+            int k = (int)std::ceil(c / h->maxCfl);
+            *substeps = k > 1 ? k : 1;
+        }
+    });
 }
 
 astg_status astg_set_reduction_order(astg_handle* h, astg_order order, int workers) {

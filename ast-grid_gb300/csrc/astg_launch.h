@@ -198,6 +198,8 @@ struct LevelSpans {
 cudaError_t launch_mean_temperature_static(const double* heat, const LevelSpans& sp, double* amb, cudaStream_t st);
 // the same in the reference's order (BLAS::sum's per-worker slices, `workers` workers)
 void launch_mean_temperature_ref(const Dev& d, const double* hO, int workers, double* amb, cudaStream_t st);
+// largest positive MAC face value (0 when none) into *out (which must start at 0)
+void launch_max_face(const Dev& d, const double* mac, unsigned long long* out, cudaStream_t st);
 void launch_force(const Dev& d, const Fields& F, const uint8_t* open, const double* amb, double dt, cudaStream_t st);
 void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);
 void launch_velocity_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);

@@ -672,4 +672,23 @@ void launch_advect_velocity(const Dev& d, const Fields& cur, const Fields& nxt, 
 }
 void launch_decay(const Dev& d, const Fields& F, cudaStream_t st) { ASTG_LAUNCH(k_decay<<<nblk(d.S), TB, 0, st>>>(d, F)); }
 
+// Largest MAC face value over all faces (3 x slots, ghosts included), starting from 0, as
+// OctreeOmniGridSolver3::cfl takes it (src/octree_omnigrid_solver3.cpp:1066-1122): only positive
+// values can raise it, and for those the IEEE bit patterns order like the values, so the maximum
+// is an atomicMax on the bits (order-independent, exact).  *out must start at 0.
+__global__ void k_max_face(const double* mac, long long n, unsigned long long* out) {
+    unsigned long long m = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double v = mac[i];
+        if (v > 0) m = max(m, (unsigned long long)__double_as_longlong(v));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(out, m);
+}
+void launch_max_face(const Dev& d, const double* mac, unsigned long long* out, cudaStream_t st) {
+    long long n = 3LL * d.S;
+    int blocks = (int)std::min<long long>(nblk(n), 4LL * 152);
+    ASTG_LAUNCH(k_max_face<<<blocks, TB, 0, st>>>(mac, n, out));
+}
+
 }  // namespace astg

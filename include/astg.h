@@ -96,6 +96,22 @@ const char* astg_last_error(const astg_handle* h);
  * OctreeOmniGridSolver3::onUpdate (src/octree_omnigrid_solver3.cpp:222-249). */
 astg_status astg_step(astg_handle* h, double dt, astg_step_stats* stats);
 
+/* Solver::update(dt) with useFixedTimeStep = false (src/solver.cpp:21-41), the reference's default:
+ * the frame is split into sub-steps of remaining / k, k = numberOfSubTimeSteps(remaining) =
+ * max(1, ceil(cfl(remaining) / maxCfl)) recomputed from the current velocity before each sub-step,
+ * until at most EPSILON remains (src/octree_omnigrid_solver3.cpp:1060-1063).  *substeps (may be
+ * NULL) receives the number of sub-steps; stats are the last sub-step's, with the times summed over
+ * the frame.  ASTG_NOT_CONVERGED when any sub-step's solve did not converge. */
+astg_status astg_update(astg_handle* h, double dt, int* substeps, astg_step_stats* stats);
+
+/* setMaxCfl (include/octree_omnigrid_solver3.h:29); the default is the reference's 3. */
+astg_status astg_set_max_cfl(astg_handle* h, double max_cfl);
+
+/* OctreeOmniGridSolver3::cfl(dt) (src/octree_omnigrid_solver3.cpp:1066-1122: dt times the largest
+ * MAC face value, counted from 0, over the finest spacing, truncated to int) and
+ * numberOfSubTimeSteps(dt) for the current velocity; either pointer may be NULL. */
+astg_status astg_cfl(astg_handle* h, double dt, int* cfl, int* substeps);
+
 /* One stage of onUpdate: 0 scene setup (source), 1 addForce, 2 wall constraint + velocity ghosts,
  * 3 project (:350-679), 4 constraint + ghosts + dual grid, 5 advect (:850-914). */
 astg_status astg_stage(astg_handle* h, int stage, double dt);

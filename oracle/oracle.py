@@ -70,6 +70,9 @@ def lib(openmp=False):
         _lib.orc_destroy.argtypes = [ctypes.c_void_p]
         _lib.orc_stage.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_char_p, ctypes.c_int]
         _lib.orc_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_char_p, ctypes.c_int]
+        _lib.orc_update.restype = ctypes.c_int
+        _lib.orc_update.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_int,
+                                    ctypes.c_char_p, ctypes.c_int]
         _lib.orc_get.restype = ctypes.c_longlong
         _lib.orc_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_longlong]
         _lib.orc_set.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_longlong]
@@ -119,6 +122,15 @@ class Oracle:
     def step(self, dt):
         err = ctypes.create_string_buffer(512)
         self._check(self._lib.orc_step(self._h, dt, err, 512), err)
+
+    def update(self, dt, max_cfl=3.0):
+        """Solver::update with useFixedTimeStep = false (CFL sub-steps); returns the sub-step counts."""
+        err = ctypes.create_string_buffer(512)
+        buf = (ctypes.c_int * 4096)()
+        n = self._lib.orc_update(self._h, dt, max_cfl, buf, 4096, err, 512)
+        if n < 0:
+            raise RuntimeError("oracle: " + err.value.decode())
+        return list(buf[:n])
 
     def get(self, name):
         n = self._lib.orc_get(self._h, name.encode(), None, 0)

@@ -17,7 +17,7 @@
 //
 // usage: ref_harness --coarsest N --levels L --steps S --out DIR [--dt 0.01] [--tol 1e-6]
 //        [--noise 1e-3] [--seed 0] [--buoy-d -0.1] [--buoy-t 1.0] [--decay 1.0] [--stages]
-//        [--source cx,cy,cz,r]
+//        [--source cx,cy,cz,r] [--adaptive] [--max-cfl C]
 #include "octree_omnigrid_solver3.h"
 #include "octree_util.h"
 #include "advection.h"
@@ -45,6 +45,9 @@ struct Options {
     double dt = 0.01, tol = 1e-6, noise = 1e-3, buoyD = -0.1, buoyT = 1.0, decay = 1.0;
     uint64_t seed = 0;
     bool stages = false;
+    // Solver::update's adaptive branch (useFixedTimeStep = false) with setMaxCfl(maxCfl)
+    bool adaptive = false;
+    double maxCfl = 3.0;
     // FmmLevelSetSolver3::extrapolate of the density after the steps: sphere SDF (centre, radius),
     // maximum distance factor, validity offset (known where sdf < -offset * d)
     // checkpoint: after step ckptAt, write the reference's own binary dumps into ckptDir; restart:
@@ -76,7 +79,8 @@ public:
         _smokeDecayFactor = o.decay;
         _temperatureDecayFactor = o.decay;
         isRestart = true;  // only suppresses the layout.bin dump in initData (:147-148)
-        useFixedTimeStep = true;
+        useFixedTimeStep = !o.adaptive;
+        if (o.adaptive) setMaxCfl(o.maxCfl);
         numOctreeLayer = o.levels;
         split = astg_scene::split_map(res, o.levels, o.src);
         splitMapSetup = [this, res](OctreeOmniGridSolver3* s) {
@@ -95,6 +99,13 @@ public:
         boundarySdf = boundarySolver->colliderSdf();
     }
     void saveResult(int) override {}
+    // sub-step counts the adaptive update computed during the current frame
+    mutable std::vector<int> subLog;
+    int numberOfSubTimeSteps(REAL dt) const override {
+        int k = OctreeOmniGridSolver3::numberOfSubTimeSteps(dt);
+        subLog.push_back(k);
+        return k;
+    }
 
     bool inSrc(const Vector3f& p) const { return astg_scene::inside(opt.src, p.x(), p.y(), p.z()); }
 
@@ -429,6 +440,8 @@ int main(int argc, char** argv) {
         else if (a == "--buoy-t") o.buoyT = atof(next());
         else if (a == "--decay") o.decay = atof(next());
         else if (a == "--stages") o.stages = true;
+        else if (a == "--adaptive") o.adaptive = true;
+        else if (a == "--max-cfl") o.maxCfl = atof(next());
         else if (a == "--out") o.out = next();
         else if (a == "--source") parseSource(next(), o.src);
         else if (a == "--checkpoint-at") o.ckptAt = atoi(next());
@@ -469,6 +482,7 @@ int main(int argc, char** argv) {
     for (int s = 0; s < o.steps; ++s) {
         h.stepIdx = s;
         h.stageAr.entries.clear();
+        h.subLog.clear();
         Timer t;
         h.update(o.dt);
         double secs = t.durationInSeconds();
@@ -476,6 +490,7 @@ int main(int argc, char** argv) {
         h.dumpState(st, "");
         h.dumpProjection(st, "");
         st.f64("wall_s", std::vector<double>{secs});
+        if (o.adaptive) st.i32("substeps", h.subLog);
         char name[64];
         snprintf(name, sizeof name, "/step_%04d.astg", s + 1);
         st.write(o.out + name);

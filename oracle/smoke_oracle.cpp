@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <limits>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -1912,6 +1913,35 @@ public:
     void step(double dt) {
         for (int i = 0; i < 6; ++i) stage(i, dt);
     }
+    // OctreeOmniGridSolver3::cfl (src/octree_omnigrid_solver3.cpp:1066-1122): the largest MAC face
+    // value over all faces of all levels (ghost slots included, starting from 0, so negative
+    // values never count), times dt over the finest spacing, truncated to int
+    int cfl(double dt) const {
+        double maxV = 0;
+        for (int a = 0; a < 3; ++a)
+            for (double v : mac[cur][a]) maxV = std::max(maxV, v);
+        return (int)(dt * maxV / dx);
+    }
+    // numberOfSubTimeSteps (:1060-1063)
+    int numberOfSubTimeSteps(double dt, double maxCfl) const {
+        int k = (int)std::ceil(cfl(dt) / maxCfl);
+        return k > 1 ? k : 1;
+    }
+    // Solver::update's adaptive branch (src/solver.cpp:21-41, useFixedTimeStep = false): sub-steps
+    // of remaining / k until less than EPSILON (general.h:48) remains, k recomputed from the
+    // current velocity before each sub-step; returns the sub-step counts in order
+    std::vector<int> update(double dt, double maxCfl) {
+        std::vector<int> ks;
+        double remaining = dt;
+        while (remaining > std::numeric_limits<double>::epsilon()) {
+            int k = numberOfSubTimeSteps(remaining, maxCfl);
+            ks.push_back(k);
+            double actual = remaining / (double)k;
+            step(actual);
+            remaining -= actual;
+        }
+        return ks;
+    }
     void finishInit() {
         halfMark.assign(S, 0);
         for (int hs : halfTilts) halfMark[hs] = 1;
@@ -2182,6 +2212,19 @@ int orc_step(void* h, double dt, char* err, int errlen) {
     } catch (std::exception& e) {
         if (err && errlen > 0) snprintf(err, errlen, "%s", e.what());
         return 1;
+    }
+}
+
+// Solver::update with useFixedTimeStep = false: writes the sub-step counts (at most cap) to
+// substeps and returns how many there were, or -1 on failure
+int orc_update(void* h, double dt, double max_cfl, int* substeps, int cap, char* err, int errlen) {
+    try {
+        std::vector<int> ks = ((oracle::Solver*)h)->update(dt, max_cfl);
+        for (int i = 0; i < (int)ks.size() && i < cap; ++i) substeps[i] = ks[i];
+        return (int)ks.size();
+    } catch (std::exception& e) {
+        if (err && errlen > 0) snprintf(err, errlen, "%s", e.what());
+        return -1;
     }
 }
 

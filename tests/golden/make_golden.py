@@ -73,6 +73,13 @@ CKPT_CASES = [
     # name, coarsest, levels, steps before the checkpoint
     ("ref_ckpt_c8_l3", 8, 3, 2),
 ]
+CFL_CASES = [
+    # name, coarsest, levels, frames, frame time step, maxCfl: Solver::update's adaptive branch
+    # (useFixedTimeStep = false, setMaxCfl), the sub-step counts the reference computed per frame
+    ("ref_cfl_c8_l3", 8, 3, 6, 0.25, 2.0),
+]
+CFL_KEYS = ["density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
+            "tilt_e", "tilt_flags", "tilt_open", "pindex_oct", "pindex_tilt", "p", "pcg_iters", "substeps"]
 EXTRAP_CASES = [
     # name, coarsest, levels, steps, (centre x, y, z, radius, max distance factor, validity offset)
     ("ref_extrap_c8_l3", 8, 3, 2, (0.47, 0.53, 0.29, 0.15, 4.0, 0.0)),
@@ -225,6 +232,24 @@ def ckpt_fixtures(harness):
             print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB, {len(out)} arrays")
 
 
+def cfl_fixtures(harness):
+    for name, c, lv, frames, dt, max_cfl in CFL_CASES:
+        with tempfile.TemporaryDirectory() as d:
+            subprocess.check_call([harness, "--coarsest", str(c), "--levels", str(lv), "--steps", str(frames),
+                                   "--dt", repr(dt), "--adaptive", "--max-cfl", repr(max_cfl), "--out", d],
+                                  stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            out = {}
+            for k in range(1, frames + 1):
+                st = astg_archive.read(os.path.join(d, f"step_{k:04d}.astg"))
+                for key in CFL_KEYS:
+                    out[f"frame{k}/{key}"] = st[key]
+            out["meta/case"] = np.array([c, lv, frames], dtype=np.int32)
+            out["meta/adaptive"] = np.array([dt, max_cfl])
+            path = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(path, **out)
+            print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB, {len(out)} arrays")
+
+
 def main():
     ref = os.environ.get("ASTG_REF", os.path.join(os.path.dirname(ROOT), "reference"))
     subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "ref", "Makefile"), f"REF={ref}",
@@ -232,6 +257,9 @@ def main():
     harness = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
     if "--hashes-3d" in sys.argv:
         hashes_3d(harness)
+        return
+    if "--cfl-only" in sys.argv:
+        cfl_fixtures(harness)
         return
     if "--2d-only" in sys.argv:
         fixtures_2d()

@@ -130,3 +130,22 @@ def test_full_size_hashes_match_reference(name):
         got = make_golden.step_hashes(o.get)
         bad = [f for f in got if got[f] != rec["steps"][k][f]]
         assert not bad, f"step {k + 1}: {bad}"
+
+
+def test_adaptive_substeps_bit_exact():
+    """Solver::update's adaptive branch (useFixedTimeStep = false, setMaxCfl(2); src/solver.cpp:21-41,
+    numberOfSubTimeSteps / cfl at src/octree_omnigrid_solver3.cpp:1060-1122) for six frames of dt 0.25:
+    the oracle takes the reference's sub-step counts and reproduces every field after each frame."""
+    g = golden("ref_cfl_c8_l3")
+    c, lv, frames = case("ref_cfl_c8_l3")
+    dt, max_cfl = g["meta/adaptive"].tolist()
+    o = Oracle(c, lv)
+    counts = []
+    for k in range(1, frames + 1):
+        ks = o.update(dt, max_cfl)
+        st = state(g, f"frame{k}/")
+        assert ks == st["substeps"].tolist(), f"frame {k}"
+        counts += ks
+        for f in FIELDS + ["tilt_open", "pindex_oct", "pindex_tilt", "p", "pcg_iters"]:
+            assert_same(f"frame{k}/{f}", st[f], o.get(f))
+    assert max(counts) >= 3  # the case does sub-step
