@@ -17,7 +17,7 @@
 //
 // usage: ref_harness --coarsest N --levels L --steps S --out DIR [--dt 0.01] [--tol 1e-6]
 //        [--noise 1e-3] [--seed 0] [--buoy-d -0.1] [--buoy-t 1.0] [--decay 1.0] [--stages]
-//        [--source cx,cy,cz,r] [--adaptive] [--max-cfl C]
+//        [--source cx,cy,cz,r] [--adaptive] [--max-cfl C] [--collider cx,cy,cz,r]
 #include "octree_omnigrid_solver3.h"
 #include "octree_util.h"
 #include "advection.h"
@@ -25,6 +25,8 @@
 #include "viewer/grid_dump.h"
 #include "scene.h"
 #include "archive.h"
+#include "geometry/sphere3.h"
+#include "geometry/rigid_body_collider3.h"
 
 #include <cstdio>
 #include <cstdlib>
@@ -48,6 +50,10 @@ struct Options {
     // Solver::update's adaptive branch (useFixedTimeStep = false) with setMaxCfl(maxCfl)
     bool adaptive = false;
     double maxCfl = 3.0;
+    // a sphere collider through OmniBoundarySolver3::updateCollider (the stock scene's obstacle
+    // code path, src/omni_boundary_solver3.cpp:17-32, src/octree_omnigrid_solver3.cpp:153-158)
+    bool collider = false;
+    double col[4] = {0.5, 0.5, 0.45, 0.1};
     // FmmLevelSetSolver3::extrapolate of the density after the steps: sphere SDF (centre, radius),
     // maximum distance factor, validity offset (known where sdf < -offset * d)
     // checkpoint: after step ckptAt, write the reference's own binary dumps into ckptDir; restart:
@@ -96,6 +102,10 @@ public:
     void initObstacle() override {
         boundarySolver->setClosedDomainBoundaryFlag(kDirectionXNegative | kDirectionXPositive | kDirectionYNegative |
                                                     kDirectionYPositive | kDirectionZNegative);
+        if (opt.collider) {
+            Sphere3Ptr sphere = std::make_shared<Sphere3>(opt.col[3], Transform3(Vector3f(opt.col[0], opt.col[1], opt.col[2]), Quaternion()));
+            boundarySolver->updateCollider(std::make_shared<RigidBodyCollider3>(sphere));
+        }
         boundarySdf = boundarySolver->colliderSdf();
     }
     void saveResult(int) override {}
@@ -248,6 +258,14 @@ public:
         ar.i32("level_sizes", sizes, {(uint64_t)levels(), 3});
         ar.i32("slot_coords", coords, {(uint64_t)(coords.size() / 4), 4});
         ar.i32("split_map", split);
+        if (opt.collider) {  // the collider SDF grid the solver samples, index (z * res + y) * res + x
+            int r = resolution.x();
+            std::vector<double> sd((size_t)r * r * r);
+            for (int z = 0; z < r; ++z)
+                for (int y = 0; y < r; ++y)
+                    for (int x = 0; x < r; ++x) sd[((size_t)z * r + y) * r + x] = boundarySdf->get(x, y, z);
+            ar.f64("collider_sdf", sd);
+        }
         auto toVec = [](const std::vector<LCOOR_T>& v) { return std::vector<int64_t>(v.begin(), v.end()); };
         ar.i64("half_tilts", toVec(layout->getHalfGhostIdx()));
         std::vector<int64_t> tj = toVec(layout->getTJointArr());
@@ -442,6 +460,11 @@ int main(int argc, char** argv) {
         else if (a == "--stages") o.stages = true;
         else if (a == "--adaptive") o.adaptive = true;
         else if (a == "--max-cfl") o.maxCfl = atof(next());
+        else if (a == "--collider") {
+            o.collider = true;
+            if (sscanf(next(), "%lf,%lf,%lf,%lf", &o.col[0], &o.col[1], &o.col[2], &o.col[3]) != 4)
+                throw std::runtime_error("--collider cx,cy,cz,r");
+        }
         else if (a == "--out") o.out = next();
         else if (a == "--source") parseSource(next(), o.src);
         else if (a == "--checkpoint-at") o.ckptAt = atoi(next());

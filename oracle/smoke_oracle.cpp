@@ -305,6 +305,13 @@ public:
     std::vector<int> halfTilts, tJoints, closedByHalf;  // slots
     std::vector<double> wMac[3];
     std::vector<double> wTilt;  // S*8
+    // Collider: OmniBoundarySolver3's SDF grid (res^3 finest cells, spacing dx, index
+    // (z*res + y)*res + x; src/omni_boundary_solver3.cpp:11-32); empty = no collider (the reference's
+    // grid filled with 1, on which every test below is false).  colCentre is the centre the
+    // inside-solid projection takes its normals from, hard-coded (0.5, 0.5, 0.45) in the reference
+    // (include/omni_boundary_solver3.h:27,57,77).
+    std::vector<double> colSdf;
+    V3 colCentre{0.5, 0.5, 0.45};
     double M37[128][3][7];      // OCTREE_OMNI_DUAL_GRAPH_EIGEN_MATRIX3, bits x y z n0 n1 n2 n3
     int anomalies = 0;          // lookups the reference would have inserted into its hash map
 
@@ -706,26 +713,175 @@ public:
                 tiltE[1][s] = n;
             }
         }
-        // cut-cell weights for a collider-free domain: every face weight is 1 - 0; the
-        // half-tilt vectors start from zero and get 1 on the slots the reference fills
+        cuttingCellWeights();
+        cur = 0;
+        firstSource = true;
+    }
+
+    // ---------------------------------------------------------------- collider
+    // boundarySdf->sample(p): CellCenteredGrid<REAL,3>::sample of the collider grid, or the
+    // reference's constant 1 without a collider
+    double bsdf(const V3& p) const { return colSdf.empty() ? 1.0 : sdfSample(colSdf, res, p); }
+    // fractionInside, include/util.h:340-349
+    static double fractionInside(double l, double r) {
+        if (l < 0 && r < 0) return 1;
+        if (l < 0 && r >= 0) return l / (l - r);
+        if (l >= 0 && r < 0) return r / (r - l);
+        return 0;
+    }
+    // isInsideSdf, include/util.h:324
+    static bool insideSdf(double phi) { return phi <= 0; }
+    V3 octPosL(int l, int x, int y, int z) const {
+        double h = dh(l);
+        return v3(x * h + 0.5 * h, y * h + 0.5 * h, z * h + 0.5 * h);
+    }
+    // initCuttingCellWeights, src/octree_omnigrid_solver3.cpp:1169-1238 (weightsCC->setAll(1) first,
+    // :83): MAC faces and tilt slots of non-ghost nodes get 1 - fractionInside of the SDF at the two
+    // octagon centres (tilt centre and octagon centre) when the neighbouring octagon is valid; a half
+    // tilt starts from zero and fills its big-octagon slot and its four same-level slots.  Two
+    // quirks are kept: the big octagon's position is taken at the half tilt's own level with the
+    // coarse index, and the same-level slots sample the SDF at the last position computed (the big
+    // octagon's when it was valid, else the half tilt's centre), not at their own octagon.
+    void cuttingCellWeights() {
         for (int a = 0; a < 3; ++a) wMac[a].assign(S, 1.0);
         wTilt.assign((size_t)S * 8, 1.0);
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & F_GHOST) continue;
+            int l = slev[s], x = sx[s], y = sy[s], z = sz[s];
+            double current = bsdf(octPosL(l, x, y, z));
+            for (int a = 0; a < 3; ++a) {
+                int id[3] = {x, y, z};
+                id[a] -= 1;
+                if (macValid(a, l, x, y, z) && octValid(l, id[0], id[1], id[2]))
+                    wMac[a][s] = 1 - fractionInside(bsdf(octPosL(l, id[0], id[1], id[2])), current);
+            }
+        }
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & F_GHOST) continue;
+            int l = slev[s];
+            double current = bsdf(vertPos(s));
+            for (int i = 0; i < 8; ++i) {
+                int nx = sx[s] + TILT_NB_OCT[i][0], ny = sy[s] + TILT_NB_OCT[i][1], nz = sz[s] + TILT_NB_OCT[i][2];
+                if (octValid(l, nx, ny, nz))
+                    wTilt[(size_t)s * 8 + i] = 1 - fractionInside(current, bsdf(octPosL(l, nx, ny, nz)));
+            }
+        }
         for (int hs : halfTilts) {
             double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             const TiltE& n = tiltE[0][hs];
             int l = slev[hs];
+            V3 pos = vertPos(hs);
+            double current = bsdf(pos);
             int id[3] = {sx[hs] >> 1, sy[hs] >> 1, sz[hs] >> 1};
             id[n.dir % 3] -= n.dir < 3 ? 1 : 0;
-            if (l + 1 < L && octValid(l + 1, id[0], id[1], id[2])) w[HALF_SLOT[n.dir][4]] = 1.0;
+            if (l + 1 < L && octValid(l + 1, id[0], id[1], id[2])) {
+                pos = octPosL(l, id[0], id[1], id[2]);
+                w[HALF_SLOT[n.dir][4]] = 1 - fractionInside(current, bsdf(pos));
+            }
             for (int i = 0; i < 4; ++i) {
                 int k = HALF_SLOT[n.dir][i];
                 if (octValid(l, sx[hs] + TILT_NB_OCT[k][0], sy[hs] + TILT_NB_OCT[k][1], sz[hs] + TILT_NB_OCT[k][2]))
-                    w[k] = 1.0;
+                    w[k] = 1 - fractionInside(current, bsdf(pos));
             }
             for (int k = 0; k < 8; ++k) wTilt[(size_t)hs * 8 + k] = w[k];
         }
-        cur = 0;
-        firstSource = true;
+    }
+    // wipeBoundary, src/octree_omnigrid_solver3.cpp:1240-1293 (EXTRAPOLATE_DENSITY undefined): density
+    // and heat of non-ghost octagons and tilts and of half tilts whose position has SDF < 0 become
+    // 0 / EPSILON = 0
+    void wipeBoundary() {
+        if (colSdf.empty()) return;
+        int c = cur;
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & F_GHOST) continue;
+            if (bsdf(cellPos(s)) < 0) { dO[c][s] = 0.0 / DBL_EPSILON; hO[c][s] = 0.0 / DBL_EPSILON; }
+        }
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & F_GHOST) continue;
+            if (bsdf(vertPos(s)) < 0) { dT[c][s] = 0.0 / DBL_EPSILON; hT[c][s] = 0.0 / DBL_EPSILON; }
+        }
+        for (int hs : halfTilts)
+            if (bsdf(vertPos(hs)) < 0) { dT[c][hs] = 0; hT[c][hs] = 0; }
+    }
+    // Eigen 3.3.7 on 3-vectors (no packet access: the unrolled redux splits the range in halves,
+    // Eigen/src/Core/Redux.h:91-105, so a sum of three terms is t0 + (t1 + t2)): the norm, and the
+    // tangential part v - (v . n) n with n normalised by normalize() (division by sqrt of the squared
+    // norm when it is positive, Eigen/src/Core/Dot.h:145-151)
+    static double sq3(const V3& n) { return n.x * n.x + (n.y * n.y + n.z * n.z); }
+    static double norm3(const V3& n) { return std::sqrt(sq3(n)); }
+    static V3 tangential(const V3& v, V3 n) {
+        double z = sq3(n);
+        if (z > 0) {
+            double q = std::sqrt(z);
+            n = v3(n.x / q, n.y / q, n.z / q);
+        }
+        double d = v.x * n.x + (v.y * n.y + v.z * n.z);
+        return v3(v.x - d * n.x, v.y - d * n.y, v.z - d * n.z);
+    }
+    // OmniBoundarySolver3::constrainVelocity(MAC grid), include/omni_boundary_solver3.h:74-92: each valid
+    // face of a non-ghost node inside the solid (SDF <= 0) becomes the matching component of the
+    // tangential part of the MAC velocity sampled there, or 0 at the centre itself.  The reference's
+    // loop writes the grid it samples from one task per worker, each over a contiguous run of nodes,
+    // all at once: where the solid's faces span two runs, what a sample reads depends on thread
+    // timing.  Restated with a defined order: every sample reads the velocity as it was before this
+    // loop (it agrees with the reference wherever no sample reads another solid face).
+    void colliderMac() {
+        if (colSdf.empty()) return;
+        int c = cur;
+        std::vector<double> before[3] = {mac[c][0], mac[c][1], mac[c][2]};
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & F_GHOST) continue;
+            for (int a = 0; a < 3; ++a) {
+                if (!macValid(a, slev[s], sx[s], sy[s], sz[s])) continue;
+                V3 pos = macPos(a, s);
+                if (!insideSdf(bsdf(pos))) continue;
+                V3 n = pos - colCentre;
+                if (norm3(n) < DBL_EPSILON) {
+                    mac[c][a][s] = 0;
+                } else {
+                    V3 t = tangential(macSample(pos, before), n);
+                    mac[c][a][s] = t[a];
+                }
+            }
+        }
+    }
+    // constrainVelocity(tilt grid, MAC grid), include/omni_boundary_solver3.h:26-52: for open tilts of
+    // non-ghost nodes with SDF(centre) - dx <= 0, slot k at centre + e/3 (e = dx/2) inside the solid.
+    // The reference's projected value is written into a shadowing local Vector3f, not into the tilt,
+    // so only the degenerate case (slot position at the centre itself: v[k] = 0) changes the tilt.
+    void colliderTilt() {
+        if (colSdf.empty()) return;
+        int c = cur;
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & F_GHOST) continue;
+            if (tiltE[c][s].closed) continue;
+            V3 centre = vertPos(s);
+            double h = dh(slev[s]);
+            if (!insideSdf(bsdf(centre) - h)) continue;
+            double e = h * 0.5;
+            for (int k = 0; k < 8; ++k) {
+                V3 p1 = tiltPos(centre, k, e);
+                if (insideSdf(bsdf(p1)) && norm3(p1 - colCentre) < DBL_EPSILON) tv[c][(size_t)s * 8 + k] = 0;
+            }
+        }
+    }
+    // constrainVelocity(OctreeOmniVector3Grid3), include/omni_boundary_solver3.h:55-71: the dual vectors
+    // at non-ghost tilt positions inside the solid lose their normal part (0 at the centre itself)
+    void colliderDual() {
+        if (colSdf.empty()) return;
+        int c = cur;
+        std::vector<double>& DT = dual[c][1];
+        for (int s = 0; s < S; ++s) {
+            if (sflag[s] & F_GHOST) continue;
+            V3 pos = vertPos(s);
+            if (!insideSdf(bsdf(pos))) continue;
+            V3 n = pos - colCentre;
+            V3 v = v3(DT[3 * s], DT[3 * s + 1], DT[3 * s + 2]);
+            V3 t = norm3(n) < DBL_EPSILON ? v3(0, 0, 0) : tangential(v, n);
+            DT[3 * s] = t.x;
+            DT[3 * s + 1] = t.y;
+            DT[3 * s + 2] = t.z;
+        }
     }
 
     // ---------------------------------------------------------------- positions
@@ -960,10 +1116,17 @@ public:
         return v + diff * 2 * mn;
     }
 
-    // include/advection.h:49-62 (constant +1 SDF: the boundary clamp never triggers)
+    // include/advection.h:49-62: RK2 midpoint, then the boundary clamp: when the SDF changes sign
+    // between p and the traced point, the point moves back toward p by |phi1| / (|phi0| + |phi1|)
     V3 backTrace(V3 p, double dt, int bf) {
         V3 mid = p - velSample(p, bf) * dt * 0.5;
-        return p - velSample(mid, bf) * dt;
+        V3 ret = p - velSample(mid, bf) * dt;
+        double phi0 = bsdf(p), phi1 = bsdf(ret);
+        if (phi0 * phi1 < 0.0) {
+            double w = std::fabs(phi1) / (std::fabs(phi0) + std::fabs(phi1));
+            return v3(w * p.x + (1.0 - w) * ret.x, w * p.y + (1.0 - w) * ret.y, w * p.z + (1.0 - w) * ret.z);
+        }
+        return ret;
     }
 
     // ---------------------------------------------------------------- ghost updates
@@ -1269,14 +1432,16 @@ public:
     // src/octree_omnigrid_solver3.cpp:292-347 (sequential numbering in iterator order)
     void updateIndex() {
         int n = 0;
+        // a DOF only where the SDF at its position exceeds -3 dx_l (:297-309, threshold 3)
+        auto fluid = [&](int s, const V3& p) { return bsdf(p) > -dh(slev[s]) * 3.0; };
         for (int s = 0; s < S; ++s) {
             if (sflag[s] & F_GHOST) continue;
-            pO[s] = octValid(slev[s], sx[s], sy[s], sz[s]) ? n++ : -1;
-            pT[s] = tOpen[s] ? n++ : -1;
+            pO[s] = octValid(slev[s], sx[s], sy[s], sz[s]) && fluid(s, cellPos(s)) ? n++ : -1;
+            pT[s] = tOpen[s] && fluid(s, vertPos(s)) ? n++ : -1;
         }
         for (int s = 0; s < S; ++s)
             if (sflag[s] & F_GHOST) { pO[s] = -1; pT[s] = -1; }
-        for (int hs : halfTilts) pT[hs] = n++;
+        for (int hs : halfTilts) pT[hs] = fluid(hs, vertPos(hs)) ? n++ : -1;
         // OctreeVertexCenteredGrid3<int>::updateGhost, src/octree_vertex_centered_grid3.cpp:47-64
         for (int l = 0; l < L; ++l)
             for (int i = lN[l]; i < lN[l] + lG[l]; ++i) {
@@ -1902,10 +2067,13 @@ public:
     void stage(int id, double dt) {
         switch (id) {
             case 0: source(); break;
-            case 1: addForce(dt); break;
-            case 2: constrainWalls(); velocityGhost(cur); break;
+            case 1: wipeBoundary(); addForce(dt); break;
+            case 2: colliderMac(); constrainWalls(); colliderTilt(); velocityGhost(cur); break;
             case 3: updateIndex(); assemble(dt); pcg(); pressureUpdate(dt); break;
-            case 4: constrainWalls(); velocityGhost(cur); updateDual(); dualGhost(cur); break;
+            case 4:
+                colliderMac(); constrainWalls(); colliderTilt(); velocityGhost(cur);
+                updateDual(); colliderDual(); dualGhost(cur);
+                break;
             case 5: advect(dt); break;
             default: throw std::runtime_error("oracle: bad stage");
         }
@@ -2328,6 +2496,19 @@ long long orc_get(void* h, const char* name, void* buf, long long cap) {
 int orc_set(void* h, const char* name, const void* buf, long long count) {
     auto* s = (oracle::Solver*)h;
     std::string n = name;
+    if (n == "collider_sdf") {  // res^3 doubles (count 0: no collider); the cut-cell weights follow
+        long long r = s->res;
+        if (count != 0 && count != r * r * r) return 1;
+        s->colSdf.assign((const double*)buf, (const double*)buf + count);
+        s->cuttingCellWeights();
+        return 0;
+    }
+    if (n == "collider_centre") {
+        if (count != 3) return 1;
+        const double* c3 = (const double*)buf;
+        s->colCentre = oracle::v3(c3[0], c3[1], c3[2]);
+        return 0;
+    }
     int c = s->cur;
     static const char* fields[] = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel",
                                    "dual_oct", "dual_tilt", "tilt_e", "tilt_flags", "tilt_open"};

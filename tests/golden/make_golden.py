@@ -73,6 +73,13 @@ CKPT_CASES = [
     # name, coarsest, levels, steps before the checkpoint
     ("ref_ckpt_c8_l3", 8, 3, 2),
 ]
+COLLIDER_CASES = [
+    # the stock scene's obstacle (src/octree_omnigrid_solver3.cpp:157-158): a sphere r = 0.1 at
+    # (0.5, 0.5, 0.45) through OmniBoundarySolver3::updateCollider, in the benchmark scene
+    ("ref_col_c8_l3", 8, 3, 4, True),
+    ("ref_col_c16_l2", 16, 2, 3, False),
+]
+COLLIDER = ["--collider", "0.5,0.5,0.45,0.1"]
 CFL_CASES = [
     # name, coarsest, levels, frames, frame time step, maxCfl: Solver::update's adaptive branch
     # (useFixedTimeStep = false, setMaxCfl), the sub-step counts the reference computed per frame
@@ -258,6 +265,9 @@ def main():
     if "--hashes-3d" in sys.argv:
         hashes_3d(harness)
         return
+    if "--collider-only" in sys.argv:
+        run_cases(harness, COLLIDER_CASES, COLLIDER)
+        return
     if "--cfl-only" in sys.argv:
         cfl_fixtures(harness)
         return
@@ -272,9 +282,13 @@ def main():
     ckpt_fixtures(harness)
     if "--ckpt-only" in sys.argv:
         return
-    for name, c, lv, steps, stages in CASES:
+    run_cases(harness, CASES, [])
+
+
+def run_cases(harness, cases, extra):
+    for name, c, lv, steps, stages in cases:
         with tempfile.TemporaryDirectory() as d:
-            cmd = [harness, "--coarsest", str(c), "--levels", str(lv), "--steps", str(steps), "--out", d]
+            cmd = [harness, "--coarsest", str(c), "--levels", str(lv), "--steps", str(steps), "--out", d] + extra
             if stages:
                 cmd.append("--stages")
             subprocess.check_call(cmd)

@@ -149,3 +149,68 @@ def test_adaptive_substeps_bit_exact():
         for f in FIELDS + ["tilt_open", "pindex_oct", "pindex_tilt", "p", "pcg_iters"]:
             assert_same(f"frame{k}/{f}", st[f], o.get(f))
     assert max(counts) >= 3  # the case does sub-step
+
+
+def collider_oracle(name, **kw):
+    g = golden(name)
+    c, lv, _ = case(name)
+    o = Oracle(c, lv, **kw)
+    o.set("collider_sdf", g["collider_sdf"])
+    return o, g
+
+
+def test_collider_weights_and_steps_bit_exact():
+    """The stock obstacle (a sphere r = 0.1 at (0.5, 0.5, 0.45), OmniBoundarySolver3::updateCollider) in
+    the benchmark scene: with the reference's collider SDF grid the oracle reproduces its cut-cell
+    weights (initCuttingCellWeights, src/octree_omnigrid_solver3.cpp:1169-1238) and every step --
+    wipeBoundary, the inside-solid constrainVelocity, the DOF threshold and the back-trace clamp."""
+    name = "ref_col_c8_l3"
+    o, g = collider_oracle(name)
+    c, lv, steps = case(name)
+    for k in ["w_mac", "w_tilt"]:
+        assert_same(k, g[k], o.get(k))
+    assert (g["w_mac"] < 1).sum() > 10 and (g["w_tilt"] < 1).sum() > 100
+    for k in range(1, steps + 1):
+        o.step(DT)
+        st = state(g, f"step{k}/")
+        for f in FIELDS + ["tilt_open"] + ["pindex_oct", "pindex_tilt", "A_rowptr", "A_col", "A_val", "b", "p",
+                                           "pcg_iters"]:
+            assert_same(f"step{k}/{f}", st[f], o.get(f))
+
+
+def test_collider_stages_bit_exact_from_reference_inputs():
+    o, g = collider_oracle("ref_col_c8_l3")
+    prev = state(g, "init/")
+    for i, s in enumerate(STAGES):
+        for f in FIELDS:
+            o.set(f, prev[f])
+            o.set("t_" + f, prev["t_" + f])
+        o.set("tilt_open", prev["tilt_open"])
+        o.stage(i, DT)
+        cur = state(g, f"stage1_{s}/")
+        for f in FIELDS + ["tilt_open"]:
+            assert_same(f"{s}/{f}", cur[f], o.get(f))
+        prev = cur
+
+
+def test_collider_racy_case_close_to_reference():
+    """16^3 x 2 levels: the sphere's solid faces span two of the reference's worker runs, whose
+    concurrent writes make the inside-solid projection depend on thread timing there.  The oracle's
+    order (every sample reads the velocity before the projection) gives the same cut-cell weights, DOF
+    maps and iteration counts, and fields within the race's footprint: faces 1e-3, pressure 3e-3,
+    density 1e-5 of their largest magnitudes over three steps."""
+    from fixtures import max_rel
+
+    o, g = collider_oracle("ref_col_c16_l2")
+    _, _, steps = case("ref_col_c16_l2")
+    for k in ["w_mac", "w_tilt"]:
+        assert_same(k, g[k], o.get(k))
+    for k in range(1, steps + 1):
+        o.step(DT)
+        st = state(g, f"step{k}/")
+        for f in ["tilt_open", "pindex_oct", "pindex_tilt", "A_rowptr", "A_col", "pcg_iters"]:
+            assert_same(f"step{k}/{f}", st[f], o.get(f))
+        assert max_rel(st["mac"], o.get("mac")) <= 1e-3
+        assert max_rel(st["p"], o.get("p")) <= 3e-3
+        for f in ["density_oct", "density_tilt", "heat_oct", "heat_tilt"]:
+            assert max_rel(st[f], o.get(f)) <= 1e-5, f
