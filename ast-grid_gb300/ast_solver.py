@@ -148,7 +148,7 @@ def lib(path=None):
 
 _F64 = {"kernel_ms", "density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
         "tilt_e", "w_mac", "w_tilt", "dual_tables", "A_val", "b", "p", "ambT", "source_density_oct",
-        "source_density_tilt"}
+        "source_density_tilt", "collider_sdf", "collider_centre"}
 _I64 = {"half_tilts", "t_joints", "closed_by_half_tilt"}
 _U8 = {"tilt_open"}
 _SHAPES = {"mac": (3, -1), "tilt_vel": (-1, 8), "dual_oct": (-1, 3), "dual_tilt": (-1, 3), "tilt_flags": (-1, 2),

@@ -116,6 +116,23 @@ struct Dev {
     double srcX, srcY, srcZ, srcR;
     const double* srcO;           // per slot: density the source sets on the octagon (default 1)
     const double* srcT;           // per slot: density the source sets on the tilt / half tilt
+    // collider (OmniBoundarySolver3): SDF grid res^3 at the finest cell centres, index
+    // (z * res + y) * res + x; null when there is none (the reference's grid of 1s, on which every
+    // collider test is false); per-slot COL_* bits; the centre the inside-solid projection takes
+    // its normals from
+    const double* sdf;
+    const uint16_t* colMask;
+    double colCx, colCy, colCz;
+};
+// per-slot collider bits (set once per collider)
+enum {
+    COL_OCT_FLUID = 1,    // octagon may carry a DOF: SDF at the cell centre > -3 dx_l
+    COL_TILT_FLUID = 2,   // tilt (or half tilt) may carry a DOF: SDF at the vertex > -3 dx_l
+    COL_WIPE_OCT = 4,     // wipeBoundary zeroes density and heat of the octagon (SDF < 0)
+    COL_WIPE_TILT = 8,    // ... of the tilt or half tilt
+    COL_MAC_IN = 16,      // << a: MAC face a inside the solid (SDF <= 0), three bits
+    COL_DUAL_IN = 128,    // tilt position inside the solid: the dual vector is projected
+    COL_TILT_NEAR = 256   // SDF(vertex) - dx_l <= 0: the tilt slots are tested
 };
 
 struct Fields {

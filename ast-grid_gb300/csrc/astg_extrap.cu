@@ -39,21 +39,6 @@ __device__ __forceinline__ double from_ord(unsigned long long b) {
     return __longlong_as_double((long long)((b >> 63) ? (b & 0x7fffffffffffffffull) : ~b));
 }
 
-// CellCenteredGrid<REAL,3>::sample (include/cell_centered_grid.h:40-54) on res^3, spacing 1/res
-__device__ double sdf_sample(const double* sdf, int sres, V3 p) {
-    double sd = 1.0 / sres;
-    double rp[3] = {p.x / sd - 0.5, p.y / sd - 0.5, p.z / sd - 0.5};
-    int i[3], i1[3];
-    double f[3];
-    for (int k = 0; k < 3; ++k) {
-        bary_vec(rp[k], sres - 1, &i[k], &f[k]);
-        i1[k] = min(i[k] + 1, sres - 1);
-    }
-    auto g = [&](int x, int y, int z) { return sdf[((size_t)z * sres + y) * sres + x]; };
-    return trilerp(g(i[0], i[1], i[2]), g(i1[0], i[1], i[2]), g(i[0], i1[1], i[2]), g(i1[0], i1[1], i[2]),
-                   g(i[0], i[1], i1[2]), g(i1[0], i[1], i1[2]), g(i[0], i1[1], i1[2]), g(i1[0], i1[1], i1[2]), f[0],
-                   f[1], f[2]);
-}
 
 struct XState {
     uint8_t* mark;            // 2S: node 2s octagon, 2s + 1 tilt

@@ -81,6 +81,7 @@ struct astg_handle {
     std::vector<HTilt> te[2];
     std::vector<uint8_t> tOpen, tFixed;
     std::vector<double> wMac, wTilt, M37;
+    std::vector<double> wMac0, wTilt0;  // the collider-free weights
 
     // ---------------------------------------------------------------- device
     Dev d{};
@@ -444,7 +445,8 @@ struct astg_handle {
                 te[1][s] = n;
             }
         }
-        // cut-cell weights of a collider-free domain (src/octree_omnigrid_solver3.cpp:1169-1238)
+        // cut-cell weights of a collider-free domain (src/octree_omnigrid_solver3.cpp:1169-1238); a
+        // collider set later recomputes them (setCollider), removing it restores these
         wMac.assign((size_t)3 * S, 1.0);
         wTilt.assign((size_t)8 * S, 1.0);
         for (int hs : half) {
@@ -459,6 +461,11 @@ struct astg_handle {
             }
             for (int k = 0; k < 8; ++k) wTilt[(size_t)hs * 8 + k] = w[k];
         }
+        wMac0 = wMac;
+        wTilt0 = wTilt;
+        d.colCx = 0.5;  // the centre the reference's projection hard-codes
+        d.colCy = 0.5;
+        d.colCz = 0.45;
         uploadAll();
     }
 
@@ -1027,15 +1034,18 @@ struct astg_handle {
                 }
                 break;
             case 1:
+                if (d.sdf) launch_collider_wipe(d, C, st);  // wipeBoundary (:226)
                 if (J.refOrder) launch_mean_temperature_ref(d, C.hO, refWorkers, dAmb, st);
                 else launch_mean_temperature(d, C.hO, dParts, dPartOff, partOff.data(), dAmb, st);
                 launch_force(d, C, dOpen, dAmb, dt, st);
                 break;
-            case 2: launch_walls_and_ghost(d, C, dLastWriter, st); break;
+            case 2: constrainVelocity(C); break;
             case 3: project(dt); break;
             case 4:
-                launch_walls_and_ghost(d, C, dLastWriter, st);
-                launch_dual(d, C, st);
+                constrainVelocity(C);
+                launch_dual_update(d, C, st);
+                if (d.sdf) launch_collider_dual(d, C, st);
+                launch_dual_ghost(d, C, st);
                 break;
             case 5:
                 if (P.tilt_adaptivity) launch_adjust(d, C, N, dOpen, dFixed, dt, st);
@@ -1256,6 +1266,53 @@ struct astg_handle {
     }
     void requireFrozen(const char* what) {
         if (P.tilt_adaptivity) throw std::invalid_argument(std::string(what) + ": needs tilt adaptivity off (frozen topology)");
+        if (d.sdf) throw std::invalid_argument(std::string(what) + ": reverse mode is not available with a collider");
+    }
+
+    // ---------------------------------------------------------------- collider
+    // OmniBoundarySolver3::updateCollider (src/omni_boundary_solver3.cpp:17-32) takes a shape and
+    // samples its SDF at the finest cell centres; here the caller passes that grid (res^3 doubles,
+    // index (z * res + y) * res + x), or nothing to remove the collider.  The cut-cell weights
+    // (initCuttingCellWeights, which initialize() runs right after initObstacle) are recomputed on
+    // the device and copied back so astg_get("w_mac" / "w_tilt") returns them.
+    double* dSdf = nullptr;
+    uint16_t* dColMask = nullptr;
+    int* dHalfDir = nullptr;
+    double* dMacBefore = nullptr;
+    void setCollider(const double* sdf, size_t bytes) {
+        size_t n = (size_t)res * res * res;
+        if (bytes == 0) {
+            d.sdf = nullptr;
+            d.colMask = nullptr;
+            wMac = wMac0;
+            wTilt = wTilt0;
+            up(const_cast<double*>(d.wMac), wMac.data(), wMac.size());
+            up(const_cast<double*>(d.wTilt), wTilt.data(), wTilt.size());
+            return;
+        }
+        if (bytes != 8 * n) throw std::invalid_argument("astg_set collider_sdf: expected res^3 doubles (" + std::to_string(8 * n) + " bytes)");
+        if (T.on) throw std::invalid_argument("astg_set collider_sdf: a tape is active");
+        if (!dSdf) {
+            dSdf = dalloc<double>(n);
+            dColMask = dalloc<uint16_t>(S);
+            dMacBefore = dalloc<double>((size_t)3 * S);
+            std::vector<int> dirs(H > 0 ? H : 1, 0);
+            for (int i = 0; i < H; ++i) dirs[i] = te[0][half[i]].dir;
+            dHalfDir = upload(dirs);
+        }
+        up(dSdf, sdf, n);
+        d.sdf = dSdf;
+        d.colMask = dColMask;
+        launch_collider_setup(d, dHalfDir, dColMask, const_cast<double*>(d.wMac), const_cast<double*>(d.wTilt), st);
+        down(d.wMac, wMac.data(), wMac.size());
+        down(d.wTilt, wTilt.data(), wTilt.size());
+    }
+    // constrainVelocity(MAC) + walls, constrainVelocity(tilt), velocity ghosts (onUpdate :230-232, :236-238)
+    void constrainVelocity(Fields& C) {
+        if (d.sdf) launch_collider_mac(d, C, dMacBefore, st);
+        launch_walls(d, C.mac, st);
+        if (d.sdf) launch_collider_tilt(d, C, st);
+        launch_velocity_ghost(d, C, dLastWriter, st);
     }
     // astg_stage_vjp: the current state is the stage's input
     void stageVjp(int id, double dt) {
@@ -1677,6 +1734,15 @@ struct astg_handle {
         auto need = [&](size_t nb) {
             if (bytes != nb) throw std::invalid_argument("astg_set " + name0 + ": expected " + std::to_string(nb) + " bytes");
         };
+        if (b == cur && name == "collider_sdf") { setCollider((const double*)src, bytes); return; }
+        if (b == cur && name == "collider_centre") {
+            need(24);
+            const double* c3 = (const double*)src;
+            d.colCx = c3[0];
+            d.colCy = c3[1];
+            d.colCz = c3[2];
+            return;
+        }
         if (name == "density_oct") { need(8 * (size_t)S); up(G.dO, src, S); return; }
         if (name == "density_tilt") { need(8 * (size_t)S); up(G.dT, src, S); return; }
         if (name == "heat_oct") { need(8 * (size_t)S); up(G.hO, src, S); return; }

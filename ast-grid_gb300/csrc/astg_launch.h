@@ -200,6 +200,16 @@ cudaError_t launch_mean_temperature_static(const double* heat, const LevelSpans&
 void launch_mean_temperature_ref(const Dev& d, const double* hO, int workers, double* amb, cudaStream_t st);
 // largest positive MAC face value (0 when none) into *out (which must start at 0)
 void launch_max_face(const Dev& d, const double* mac, unsigned long long* out, cudaStream_t st);
+// collider (astg_collider.cu): per-slot bits and cut-cell weights once per collider; the per-step
+// wipe and inside-solid constraints (before: 3 * S doubles of scratch for the MAC projection)
+void launch_collider_setup(const Dev& d, const int* halfDir, uint16_t* mask, double* wMac, double* wTilt,
+                           cudaStream_t st);
+void launch_collider_wipe(const Dev& d, const Fields& F, cudaStream_t st);
+void launch_collider_mac(const Dev& d, const Fields& F, double* before, cudaStream_t st);
+void launch_collider_tilt(const Dev& d, const Fields& F, cudaStream_t st);
+void launch_collider_dual(const Dev& d, const Fields& F, cudaStream_t st);
+void launch_walls(const Dev& d, double* mac, cudaStream_t st);
+void launch_dual_update(const Dev& d, const Fields& F, cudaStream_t st);
 void launch_force(const Dev& d, const Fields& F, const uint8_t* open, const double* amb, double dt, cudaStream_t st);
 void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);
 void launch_velocity_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);

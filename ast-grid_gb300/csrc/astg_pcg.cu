@@ -526,26 +526,45 @@ static void exclusive_scan(const int* in, int* out, int* bsum, int* total, long 
 // then an open tilt take the next index; ghosts get -1; half tilts are appended in list order;
 // the tilt indices are then propagated to ghosts (OctreeVertexCenteredGrid3<int>::updateGhost,
 // src/octree_vertex_centered_grid3.cpp:47-64)
+// an octagon / tilt carries a DOF when it is valid / open and, with a collider, the SDF at its position
+// exceeds -3 dx_l (:297-309)
+__device__ __forceinline__ bool dof_oct(const Dev& d, int s) {
+    return oct_valid(d, slot_l(d, s), slot_x(d, s), slot_y(d, s), slot_z(d, s)) &&
+           (!d.colMask || (d.colMask[s] & COL_OCT_FLUID));
+}
+__device__ __forceinline__ bool dof_tilt(const Dev& d, const uint8_t* open, int s) {
+    return open[s] && (!d.colMask || (d.colMask[s] & COL_TILT_FLUID));
+}
 __global__ void k_dof_count(Dev d, const uint8_t* open, int* cnt) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.S) return;
     int c = 0;
-    if (!(slot_f(d, s) & SF_GHOST)) c = (oct_valid(d, slot_l(d, s), slot_x(d, s), slot_y(d, s), slot_z(d, s)) ? 1 : 0) + (open[s] ? 1 : 0);
+    if (!(slot_f(d, s) & SF_GHOST)) c = (dof_oct(d, s) ? 1 : 0) + (dof_tilt(d, open, s) ? 1 : 0);
     cnt[s] = c;
 }
 __global__ void k_dof_assign(Dev d, const uint8_t* open, const int* base, int* pO, int* pT) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.S) return;
     if (slot_f(d, s) & SF_GHOST) { pO[s] = -1; pT[s] = -1; return; }
-    bool ov = oct_valid(d, slot_l(d, s), slot_x(d, s), slot_y(d, s), slot_z(d, s));
+    bool ov = dof_oct(d, s);
     pO[s] = ov ? base[s] : -1;
-    pT[s] = open[s] ? base[s] + (ov ? 1 : 0) : -1;
+    pT[s] = dof_tilt(d, open, s) ? base[s] + (ov ? 1 : 0) : -1;
 }
 __global__ void k_dof_half(Dev d, int* pT, const int* n0, int* nDof) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < d.H) pT[d.half[i]] = *n0 + i;
     if (i == 0) *nDof = *n0 + d.H;
 }
+// with a collider: half tilts in list order, those in the fluid numbered consecutively
+__global__ void k_dof_half_flag(Dev d, int* flag) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d.H) flag[i] = (d.colMask[d.half[i]] & COL_TILT_FLUID) ? 1 : 0;
+}
+__global__ void k_dof_half_masked(Dev d, int* pT, const int* flag, const int* base, const int* n0) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d.H) pT[d.half[i]] = flag[i] ? *n0 + base[i] : -1;
+}
+__global__ void k_dof_total(int* nDof, const int* n0, const int* nHalf) { *nDof = *n0 + *nHalf; }
 __global__ void k_dof_ghost(Dev d, int* pT, int l) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.lG[l]) return;
@@ -562,7 +581,14 @@ void launch_dof_numbering(const Dev& d, const uint8_t* open, Proj& P, cudaStream
     ASTG_LAUNCH(k_dof_count<<<nblk(d.S), TB, 0, st>>>(d, open, P.cnt));
     exclusive_scan(P.cnt, P.base, P.bsum, P.n0, d.S, st);
     ASTG_LAUNCH(k_dof_assign<<<nblk(d.S), TB, 0, st>>>(d, open, P.base, P.pO, P.pT));
-    ASTG_LAUNCH(k_dof_half<<<nblk(d.H > 0 ? d.H : 1), TB, 0, st>>>(d, P.pT, P.n0, P.nDof));
+    if (d.colMask && d.H > 0) {  // P.cnt / P.base are free again once the slots are numbered
+        ASTG_LAUNCH(k_dof_half_flag<<<nblk(d.H), TB, 0, st>>>(d, P.cnt));
+        exclusive_scan(P.cnt, P.base, P.bsum, P.nnz + 1, d.H, st);
+        ASTG_LAUNCH(k_dof_half_masked<<<nblk(d.H), TB, 0, st>>>(d, P.pT, P.cnt, P.base, P.n0));
+        ASTG_LAUNCH(k_dof_total<<<1, 1, 0, st>>>(P.nDof, P.n0, P.nnz + 1));
+    } else {
+        ASTG_LAUNCH(k_dof_half<<<nblk(d.H > 0 ? d.H : 1), TB, 0, st>>>(d, P.pT, P.n0, P.nDof));
+    }
     for (int l = 0; l < d.L; ++l)
         if (d.lG[l]) ASTG_LAUNCH(k_dof_ghost<<<nblk(d.lG[l]), TB, 0, st>>>(d, P.pT, l));
 }

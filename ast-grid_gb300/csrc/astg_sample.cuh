@@ -246,11 +246,39 @@ ASTG_HD inline V3 vel_sample(const Dev& d, V3 p, const Fields& F) {
     return v + diff * 2 * mn;
 }
 
-// BackTrace, include/advection.h:49-62.  The collider SDF of the supported scenes is the
-// constant +1, so phi0 * phi1 > 0 always and the boundary clamp never applies.
+// CellCenteredGrid<REAL,3>::sample (include/cell_centered_grid.h:40-54) on a res^3 grid of spacing
+// 1 / res, index (z * res + y) * res + x
+ASTG_HD inline double sdf_sample(const double* sdf, int sres, V3 p) {
+    double sd = 1.0 / sres;
+    double rp[3] = {p.x / sd - 0.5, p.y / sd - 0.5, p.z / sd - 0.5};
+    int i[3], i1[3];
+    double f[3];
+    for (int k = 0; k < 3; ++k) {
+        bary_vec(rp[k], sres - 1, &i[k], &f[k]);
+        i1[k] = min(i[k] + 1, sres - 1);
+    }
+    auto g = [&](int x, int y, int z) { return sdf[((size_t)z * sres + y) * sres + x]; };
+    return trilerp(g(i[0], i[1], i[2]), g(i1[0], i[1], i[2]), g(i[0], i1[1], i[2]), g(i1[0], i1[1], i[2]),
+                   g(i[0], i[1], i1[2]), g(i1[0], i[1], i1[2]), g(i[0], i1[1], i1[2]), g(i1[0], i1[1], i1[2]), f[0],
+                   f[1], f[2]);
+}
+// boundarySdf->sample(p): the collider grid, or the reference's constant 1 without a collider
+ASTG_HD inline double bsdf(const Dev& d, V3 p) { return d.sdf ? sdf_sample(d.sdf, d.res, p) : 1.0; }
+
+// BackTrace, include/advection.h:49-62: RK2 midpoint, then the boundary clamp: when the SDF changes
+// sign between p and the traced point, the point moves back toward p by |phi1| / (|phi0| + |phi1|)
+// (never without a collider: the SDF is 1 everywhere)
 ASTG_HD inline V3 back_trace(const Dev& d, V3 p, double dt, const Fields& F) {
     V3 mid = p - vel_sample(d, p, F) * dt * 0.5;
-    return p - vel_sample(d, mid, F) * dt;
+    V3 ret = p - vel_sample(d, mid, F) * dt;
+    if (d.sdf) {
+        double phi0 = bsdf(d, p), phi1 = bsdf(d, ret);
+        if (phi0 * phi1 < 0.0) {
+            double w = fabs(phi1) / (fabs(phi0) + fabs(phi1));
+            return v3(w * p.x + (1.0 - w) * ret.x, w * p.y + (1.0 - w) * ret.y, w * p.z + (1.0 - w) * ret.z);
+        }
+    }
+    return ret;
 }
 
 // tiltNeighborOctagon3, src/octree_util.cpp:172-194: the coordinates of the octagon behind

@@ -298,6 +298,7 @@ __global__ void k_tilt_ghost(Dev d, Fields F, int l) {
     }
     for (int k = 0; k < 8; ++k) F.tv[(size_t)s * 8 + k] = F.tv[(size_t)src * 8 + k];
 }
+void launch_walls(const Dev& d, double* mac, cudaStream_t st) { ASTG_LAUNCH(k_walls<<<nblk(d.S), TB, 0, st>>>(d, mac)); }
 void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st) {
     ASTG_LAUNCH(k_walls<<<nblk(d.S), TB, 0, st>>>(d, F.mac));
     launch_velocity_ghost(d, F, lastWriter, st);
@@ -497,10 +498,13 @@ __global__ void k_dual_half(Dev d, Fields F) {
     double* o = F.dualT + 3 * (size_t)hs;
     o[0] = f.x; o[1] = f.y; o[2] = f.z;
 }
-void launch_dual(const Dev& d, const Fields& F, cudaStream_t st) {
+void launch_dual_update(const Dev& d, const Fields& F, cudaStream_t st) {
     ASTG_LAUNCH(k_dual_tilt<<<nblk(d.S), TB, 0, st>>>(d, F));
     ASTG_LAUNCH(k_dual_oct<<<nblk(d.S), TB, 0, st>>>(d, F));
     if (d.H) ASTG_LAUNCH(k_dual_half<<<nblk(d.H), TB, 0, st>>>(d, F));
+}
+void launch_dual(const Dev& d, const Fields& F, cudaStream_t st) {
+    launch_dual_update(d, F, st);
     launch_dual_ghost(d, F, st);
 }
 
