@@ -26,7 +26,7 @@ FP64, MIXED = 0, 1
 
 # exported symbols of include/astg.h
 SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_update",
-           "astg_set_max_cfl", "astg_cfl", "astg_stage",
+           "astg_set_max_cfl", "astg_cfl", "astg_stage", "astg_refine_split_map",
            "astg_set_solver_parameters", "astg_set_precision", "astg_set_reduction_order", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
            "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate",
            "astg_restart", "astg_save_checkpoint", "astg_tape_start", "astg_tape_stop", "astg_adjoint_reset",
@@ -102,6 +102,7 @@ def lib(path=None):
         L.astg_set_precision.argtypes = [c_p, ctypes.c_int]
         L.astg_update.argtypes = [c_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(StepStats)]
         L.astg_set_max_cfl.argtypes = [c_p, ctypes.c_double]
+        L.astg_refine_split_map.argtypes = [c_p, ctypes.c_int, ctypes.c_int, c_p, ctypes.c_double, ctypes.c_double]
         L.astg_cfl.argtypes = [c_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.astg_set_reduction_order.argtypes = [c_p, ctypes.c_int, ctypes.c_int]
         L.astg_set_profiling.argtypes = [c_p, ctypes.c_int]
@@ -177,6 +178,22 @@ def _dtype(name):
     if base in _U8:
         return np.uint8
     return np.int32
+
+
+def refine_split_map(split_map, level, sdf, split_range):
+    """refineSplitMapByObstacleSdf (include/octree_util.h:17-47) on a res^3 split map (in place, int32,
+    index (z * res + y) * res + x) with an SDF grid of the same shape at the finest cell centres:
+    blocks of split value `level` whose centre SDF lies in split_range = (lo, hi) become level - 1."""
+    sm = np.ascontiguousarray(split_map, dtype=np.int32)
+    sd = np.ascontiguousarray(sdf, dtype=np.float64)
+    res = round(sm.size ** (1 / 3))
+    if res ** 3 != sm.size or sd.size != sm.size:
+        raise ValueError("refine_split_map: split_map and sdf must be res^3 arrays")
+    st = lib().astg_refine_split_map(sm.ctypes.data, res, int(level), sd.ctypes.data, float(split_range[0]),
+                                     float(split_range[1]))
+    if st != ASTG_OK:
+        raise AstgError(st, "resolution not divisible by 2^level, or a bad argument")
+    return sm.reshape(np.shape(split_map))
 
 
 class OctreeSmoke3:

@@ -1894,6 +1894,56 @@ astg_status astg_set_precision(astg_handle* h, astg_precision prec) {
     return ASTG_OK;
 }
 
+namespace {
+// CellCenteredGrid<REAL,3>::sample (include/cell_centered_grid.h:40-54) on the host: getBarycentric's
+// truncating, clamped form (include/util.h:243-256) and the nested lerps of trilerp (:179-187)
+double h_lerp(double a, double b, double f) { return a * (1 - f) + b * f; }
+void h_bary_vec(double x, int high, int* i, double* f) {
+    int c = (int)x;
+    if (c < 0) c = 0;
+    if (c > high - 1) c = high - 1;
+    *i = c;
+    double t = x - c;
+    *f = t < 0 ? 0 : (t > 1 ? 1 : t);
+}
+double h_sdf_sample(const double* sdf, int sres, double px, double py, double pz) {
+    double sd = 1.0 / sres;
+    double rp[3] = {px / sd - 0.5, py / sd - 0.5, pz / sd - 0.5};
+    int i[3], i1[3];
+    double f[3];
+    for (int k = 0; k < 3; ++k) {
+        h_bary_vec(rp[k], sres - 1, &i[k], &f[k]);
+        i1[k] = std::min(i[k] + 1, sres - 1);
+    }
+    auto g = [&](int x, int y, int z) { return sdf[((size_t)z * sres + y) * sres + x]; };
+    double a = h_lerp(h_lerp(g(i[0], i[1], i[2]), g(i1[0], i[1], i[2]), f[0]),
+                      h_lerp(g(i[0], i1[1], i[2]), g(i1[0], i1[1], i[2]), f[0]), f[1]);
+    double b = h_lerp(h_lerp(g(i[0], i[1], i1[2]), g(i1[0], i[1], i1[2]), f[0]),
+                      h_lerp(g(i[0], i1[1], i1[2]), g(i1[0], i1[1], i1[2]), f[0]), f[1]);
+    return h_lerp(a, b, f[2]);
+}
+}  // namespace
+
+astg_status astg_refine_split_map(int32_t* split_map, int res, int level, const double* sdf, double lo, double hi) {
+    if (!split_map || !sdf || res <= 0 || level < 1 || level > 30) return ASTG_BAD_ARG;
+    const int k = 1 << level;
+    if (res % k != 0) return ASTG_BAD_ARG;  // "resolution is not dividable by level"
+    const int cres = res >> level;
+    const double dh = (1.0 / res) * k;
+    auto at = [&](int x, int y, int z) -> int32_t& { return split_map[((size_t)z * res + y) * res + x]; };
+    for (int tz = 0; tz < cres; ++tz)
+        for (int ty = 0; ty < cres; ++ty)
+            for (int tx = 0; tx < cres; ++tx) {
+                if (at(tx << level, ty << level, tz << level) != level) continue;
+                double v = h_sdf_sample(sdf, res, (tx + 0.5) * dh, (ty + 0.5) * dh, (tz + 0.5) * dh);
+                if (v >= lo && v <= hi)
+                    for (int z = tz << level; z < (tz << level) + k; ++z)
+                        for (int y = ty << level; y < (ty << level) + k; ++y)
+                            for (int x = tx << level; x < (tx << level) + k; ++x) at(x, y, z) = level - 1;
+            }
+    return ASTG_OK;
+}
+
 astg_status astg_update(astg_handle* h, double dt, int* substeps, astg_step_stats* stats) {
     if (!h || !(dt >= 0)) return ASTG_BAD_ARG;
     astg_status s = guard(h, [&] { h->update(dt, substeps, stats); });

@@ -81,6 +81,13 @@ typedef struct astg_step_stats {
     double ms_advect;     /* tilt adaptivity, the advection of scalars and velocity, the decay */
 } astg_step_stats;
 
+/* refineSplitMapByObstacleSdf (include/octree_util.h:17-47), a host-side utility for building the
+ * split_map that astg_create takes: every block of 2^level finest cells whose split value is `level`
+ * and whose SDF, sampled at the block centre, lies in [lo, hi] is set to level - 1.  split_map and
+ * sdf are res^3 arrays (index (z * res + y) * res + x; sdf at the finest cell centres, inside the
+ * obstacle negative).  ASTG_BAD_ARG when res is not divisible by 2^level.  Needs no device. */
+astg_status astg_refine_split_map(int32_t* split_map, int res, int level, const double* sdf, double lo, double hi);
+
 /* Fills p with the benchmark defaults for a given coarsest resolution and level count. */
 void astg_default_params(astg_params* p, int coarsest, int levels);
 

@@ -18,6 +18,7 @@
 // usage: ref_harness --coarsest N --levels L --steps S --out DIR [--dt 0.01] [--tol 1e-6]
 //        [--noise 1e-3] [--seed 0] [--buoy-d -0.1] [--buoy-t 1.0] [--decay 1.0] [--stages]
 //        [--source cx,cy,cz,r] [--adaptive] [--max-cfl C] [--collider cx,cy,cz,r]
+//        [--refine-obstacle level,lo,hi]...
 #include "octree_omnigrid_solver3.h"
 #include "octree_util.h"
 #include "advection.h"
@@ -28,6 +29,7 @@
 #include "geometry/sphere3.h"
 #include "geometry/rigid_body_collider3.h"
 
+#include <array>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -54,6 +56,9 @@ struct Options {
     // code path, src/omni_boundary_solver3.cpp:17-32, src/octree_omnigrid_solver3.cpp:153-158)
     bool collider = false;
     double col[4] = {0.5, 0.5, 0.45, 0.1};
+    // refineSplitMapByObstacleSdf(splitMap, level, colliderSdf, [lo, hi]) after the scene's split map,
+    // in the order given (include/octree_util.h:17-47)
+    std::vector<std::array<double, 3>> refine;
     // FmmLevelSetSolver3::extrapolate of the density after the steps: sphere SDF (centre, radius),
     // maximum distance factor, validity offset (known where sdf < -offset * d)
     // checkpoint: after step ckptAt, write the reference's own binary dumps into ckptDir; restart:
@@ -94,6 +99,17 @@ public:
             for (int z = 0; z < res; ++z)
                 for (int y = 0; y < res; ++y)
                     for (int x = 0; x < res; ++x) sm->set(x, y, z, split[((size_t)z * res + y) * res + x]);
+            if (!opt.refine.empty()) {
+                // the collider's SDF grid, built the way initObstacle will build it
+                OmniBoundarySolver3 bs(Size3(res, res, res), 1.0 / res);
+                Sphere3Ptr sphere = std::make_shared<Sphere3>(opt.col[3], Transform3(Vector3f(opt.col[0], opt.col[1], opt.col[2]), Quaternion()));
+                bs.updateCollider(std::make_shared<RigidBodyCollider3>(sphere));
+                auto sdf = bs.colliderSdf();
+                for (auto& r : opt.refine) refineSplitMapByObstacleSdf(sm, (int)r[0], sdf, Vector2f(r[1], r[2]));
+                for (int z = 0; z < res; ++z)
+                    for (int y = 0; y < res; ++y)
+                        for (int x = 0; x < res; ++x) split[((size_t)z * res + y) * res + x] = sm->get(x, y, z);
+            }
         };
         sceneSetup = [this](OctreeOmniGridSolver3* s) { source(s); };
     }
@@ -460,7 +476,11 @@ int main(int argc, char** argv) {
         else if (a == "--stages") o.stages = true;
         else if (a == "--adaptive") o.adaptive = true;
         else if (a == "--max-cfl") o.maxCfl = atof(next());
-        else if (a == "--collider") {
+        else if (a == "--refine-obstacle") {
+            std::array<double, 3> r;
+            if (sscanf(next(), "%lf,%lf,%lf", &r[0], &r[1], &r[2]) != 3) throw std::runtime_error("--refine-obstacle level,lo,hi");
+            o.refine.push_back(r);
+        } else if (a == "--collider") {
             o.collider = true;
             if (sscanf(next(), "%lf,%lf,%lf,%lf", &o.col[0], &o.col[1], &o.col[2], &o.col[3]) != 4)
                 throw std::runtime_error("--collider cx,cy,cz,r");

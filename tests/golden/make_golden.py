@@ -80,6 +80,11 @@ COLLIDER_CASES = [
     ("ref_col_c16_l2", 16, 2, 3, False),
 ]
 COLLIDER = ["--collider", "0.5,0.5,0.45,0.1"]
+REFINE_CASES = [
+    # refineSplitMapByObstacleSdf (include/octree_util.h:17-47) applied by the reference to the scene's
+    # split map with the stock sphere obstacle's SDF: (level, lo, hi) in order, coarse to fine
+    ("ref_refine_c16_l3", 16, 3, [(2, -1000.0, 0.3), (1, -1000.0, 0.05)]),
+]
 CFL_CASES = [
     # name, coarsest, levels, frames, frame time step, maxCfl: Solver::update's adaptive branch
     # (useFixedTimeStep = false, setMaxCfl), the sub-step counts the reference computed per frame
@@ -239,6 +244,21 @@ def ckpt_fixtures(harness):
             print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB, {len(out)} arrays")
 
 
+def refine_fixtures(harness):
+    for name, c, lv, ranges in REFINE_CASES:
+        with tempfile.TemporaryDirectory() as d:
+            cmd = [harness, "--coarsest", str(c), "--levels", str(lv), "--steps", "0", "--out", d] + COLLIDER
+            for r in ranges:
+                cmd += ["--refine-obstacle", ",".join(repr(x) for x in r)]
+            subprocess.check_call(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            lay = astg_archive.read(os.path.join(d, "layout.astg"))
+            out = {"split_map": lay["split_map"], "collider_sdf": lay["collider_sdf"],
+                   "meta/case": np.array([c, lv, 0], dtype=np.int32), "meta/refine": np.array(ranges)}
+            path = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(path, **out)
+            print(f"{path}: {os.path.getsize(path) / 1e6:.2f} MB")
+
+
 def cfl_fixtures(harness):
     for name, c, lv, frames, dt, max_cfl in CFL_CASES:
         with tempfile.TemporaryDirectory() as d:
@@ -267,6 +287,7 @@ def main():
         return
     if "--collider-only" in sys.argv:
         run_cases(harness, COLLIDER_CASES, COLLIDER)
+        refine_fixtures(harness)
         return
     if "--cfl-only" in sys.argv:
         cfl_fixtures(harness)

@@ -80,3 +80,33 @@ def test_headers_compile_as_c99(tmp_path, header):
     r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
                         "-c", str(src), "-o", str(tmp_path / "h.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_refine_split_map_matches_reference():
+    """astg_refine_split_map (host-side, no device) against the reference's own
+    refineSplitMapByObstacleSdf (include/octree_util.h:17-47) on the scene's split map with the stock
+    sphere obstacle's SDF grid, two passes coarse to fine."""
+    import ctypes
+
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from fixtures import golden
+    from oracle.oracle import Oracle
+
+    g = golden("ref_refine_c16_l3")
+    c, lv, _ = g["meta/case"].tolist()
+    res = c << (lv - 1)
+    split = np.ascontiguousarray(Oracle(c, lv).get("split_map"), dtype=np.int32)
+    sdf = np.ascontiguousarray(g["collider_sdf"], dtype=np.float64)
+    import build_lib
+
+    L = ctypes.CDLL(build_lib.build())
+    L.astg_refine_split_map.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_double,
+                                        ctypes.c_double]
+    before = split.copy()
+    for level, lo, hi in g["meta/refine"].tolist():
+        assert L.astg_refine_split_map(split.ctypes.data, res, int(level), sdf.ctypes.data, lo, hi) == 0
+    assert (split != before).sum() > 100
+    assert np.array_equal(split, g["split_map"].ravel())
+    assert L.astg_refine_split_map(split.ctypes.data, res - 1, 1, sdf.ctypes.data, 0.0, 1.0) == 1
