@@ -166,6 +166,10 @@ long long astg_size(const astg_handle* h, int what);
  *   5 half tilt; half direction)  tilt_open (u8, slots: bit 0 open, bit 1 fixed)
  *   source_density_oct source_density_tilt (f64, slots: density the source sets, default 1)
  *   prefix "t_" = the swap-partner buffer of the reference's double-buffered grids;
+ * write only: collider_sdf (f64, res^3 at the finest cell centres, index (z * res + y) * res + x:
+ *   OmniBoundarySolver3::updateCollider's SDF grid, inside negative; 0 bytes removes the collider;
+ *   the cut-cell weights are recomputed) and collider_centre (f64 x 3: the centre the inside-solid
+ *   projection takes its normals from, the reference's hard-coded (0.5, 0.5, 0.45) by default);
  * read only: slot_coords (i32, slots x 4: x y z flags) level_sizes (i32, levels x 3)
  *   half_tilts t_joints closed_by_half_tilt (i64 packed level coordinates) split_map (i32)
  *   w_mac w_tilt dual_tables (f64) pindex_oct pindex_tilt (i32) A_rowptr A_col (i32) A_val b p
