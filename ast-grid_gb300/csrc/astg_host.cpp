@@ -518,6 +518,12 @@ struct astg_handle {
             d.lres[l] = lres[l]; d.loff[l] = loff[l]; d.lN[l] = lN[l]; d.lG[l] = lG[l]; d.ldh[l] = ldh[l];
             d.brick[l] = upload(brick[l]);
         }
+        // power-of-two spacings: their reciprocals are exact, so x * (1 / h) == x / h (over_h)
+        auto pow2 = [](double v) { int e; return std::frexp(v, &e) == 0.5; };
+        d.pow2 = pow2(dx) ? 1 : 0;
+        for (int l = 0; l < L; ++l) d.pow2 = d.pow2 && pow2(ldh[l]);
+        d.dxInv = 1.0 / dx;
+        for (int l = 0; l < L; ++l) d.ldhInv[l] = 1.0 / ldh[l];
         d.locate = upload(locate);
         d.slot = upload(slot);
         d.half = upload(half);

@@ -55,9 +55,9 @@ ASTG_HD T cell_sample(const Dev& d, const G& g, V3 p) {
     int r = d.lres[l];
     int xi, yi, zi;
     double fx, fy, fz;
-    bary(p.x / h - 0.5, 0, r - 2, &xi, &fx);
-    bary(p.y / h - 0.5, 0, r - 2, &yi, &fy);
-    bary(p.z / h - 0.5, 0, r - 2, &zi, &fz);
+    bary(over_h(d, p.x, l) - 0.5, 0, r - 2, &xi, &fx);
+    bary(over_h(d, p.y, l) - 0.5, 0, r - 2, &yi, &fy);
+    bary(over_h(d, p.z, l) - 0.5, 0, r - 2, &zi, &fz);
     int x1 = imin(xi + 1, r - 2), y1 = imin(yi + 1, r - 2), z1 = imin(zi + 1, r - 2);
     return trilerp<T>(g(req(d, l, xi, yi, zi)), g(req(d, l, x1, yi, zi)), g(req(d, l, xi, y1, zi)), g(req(d, l, x1, y1, zi)),
                       g(req(d, l, xi, yi, z1)), g(req(d, l, x1, yi, z1)), g(req(d, l, xi, y1, z1)), g(req(d, l, x1, y1, z1)),
@@ -119,7 +119,7 @@ ASTG_HD T omni_sample_sub(const Dev& d, V3 p, const GO& oct, const GT& til, cons
     int l = level_of(d, p.x, p.y, p.z);
     double h = d.ldh[l];
     int r = d.lres[l];
-    double rx = p.x / h, ry = p.y / h, rz = p.z / h;
+    double rx = over_h(d, p.x, l), ry = over_h(d, p.y, l), rz = over_h(d, p.z, l);
     int xi, yi, zi;
     double fx, fy, fz;
     bary(rx, 0, r - 1, &xi, &fx);
@@ -175,9 +175,9 @@ ASTG_HD inline double scalar_sample(const Dev& d, V3 p, const double* oct, const
     int r = d.lres[l];
     int xi, yi, zi;
     double fx, fy, fz;
-    bary(p.x / h - 0.5, 0, r - 2, &xi, &fx);
-    bary(p.y / h - 0.5, 0, r - 2, &yi, &fy);
-    bary(p.z / h - 0.5, 0, r - 2, &zi, &fz);
+    bary(over_h(d, p.x, l) - 0.5, 0, r - 2, &xi, &fx);
+    bary(over_h(d, p.y, l) - 0.5, 0, r - 2, &yi, &fy);
+    bary(over_h(d, p.z, l) - 0.5, 0, r - 2, &zi, &fz);
     int x1 = imin(xi + 1, r - 2), y1 = imin(yi + 1, r - 2), z1 = imin(zi + 1, r - 2);
     int ts = req(d, l, xi + 1, yi + 1, zi + 1);
     if (near_transition(d, l, xi, yi, zi)) return omni_sample_sub<double>(d, p, ScalarAt{oct}, ScalarAt{til}, tf);
@@ -215,14 +215,14 @@ ASTG_HD inline double mac_axis(const Dev& d, int a, int l, double rx, double ry,
 ASTG_HD inline V3 mac_sample(const Dev& d, V3 p, const double* mac) {
     int l = level_of(d, p.x, p.y, p.z);
     double h = d.ldh[l];
-    double rx = p.x / h, ry = p.y / h, rz = p.z / h;
+    double rx = over_h(d, p.x, l), ry = over_h(d, p.y, l), rz = over_h(d, p.z, l);
     return v3(mac_axis(d, 0, l, rx, ry, rz, mac), mac_axis(d, 1, l, rx, ry, rz, mac + d.S),
               mac_axis(d, 2, l, rx, ry, rz, mac + 2 * (size_t)d.S));
 }
 ASTG_HD inline double mac_sample_one(const Dev& d, int a, V3 p, const double* mac) {
     int l = level_of(d, p.x, p.y, p.z);
     double h = d.ldh[l];
-    return mac_axis(d, a, l, p.x / h, p.y / h, p.z / h, mac + (size_t)a * d.S);
+    return mac_axis(d, a, l, over_h(d, p.x, l), over_h(d, p.y, l), over_h(d, p.z, l), mac + (size_t)a * d.S);
 }
 
 // OctreeOmniFaceCenteredGrid3::sample, include/octree_omni_face_centered_grid3.h:37-80
@@ -232,9 +232,9 @@ ASTG_HD inline V3 vel_sample(const Dev& d, V3 p, const Fields& F) {
     int r = d.lres[l];
     int id0, id1, id2;
     double f0, f1, f2;
-    bary_vec(p.x / h - 0.5, r - 1, &id0, &f0);
-    bary_vec(p.y / h - 0.5, r - 1, &id1, &f1);
-    bary_vec(p.z / h - 0.5, r - 1, &id2, &f2);
+    bary_vec(over_h(d, p.x, l) - 0.5, r - 1, &id0, &f0);
+    bary_vec(over_h(d, p.y, l) - 0.5, r - 1, &id1, &f1);
+    bary_vec(over_h(d, p.z, l) - 0.5, r - 1, &id2, &f2);
     int ts = req(d, l, id0 + 1, id1 + 1, id2 + 1);
     if (near_transition(d, l, id0, id1, id2)) return omni_sample_sub<V3>(d, p, Vec3At{F.dualO}, Vec3At{F.dualT}, F.tf);
     V3 v = mac_sample(d, p, F.mac);
@@ -249,8 +249,11 @@ ASTG_HD inline V3 vel_sample(const Dev& d, V3 p, const Fields& F) {
 // CellCenteredGrid<REAL,3>::sample (include/cell_centered_grid.h:40-54) on a res^3 grid of spacing
 // 1 / res, index (z * res + y) * res + x
 ASTG_HD inline double sdf_sample(const double* sdf, int sres, V3 p) {
+    // p / (1 / sres) as the reference computes it; for a power-of-two sres, p * sres is the same number
     double sd = 1.0 / sres;
-    double rp[3] = {p.x / sd - 0.5, p.y / sd - 0.5, p.z / sd - 0.5};
+    const bool p2 = (sres & (sres - 1)) == 0;
+    double rp[3] = {(p2 ? p.x * sres : p.x / sd) - 0.5, (p2 ? p.y * sres : p.y / sd) - 0.5,
+                    (p2 ? p.z * sres : p.z / sd) - 0.5};
     int i[3], i1[3];
     double f[3];
     for (int k = 0; k < 3; ++k) {
