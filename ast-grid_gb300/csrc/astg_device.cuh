@@ -151,6 +151,10 @@ struct Fields {
     double* dualT;  // S * 3
     double* te;     // tilt size e
     uint32_t* tf;   // tilt-E flag bits
+    // S * 3 or null: per tilt, the dual vector minus the MAC velocity sampled at its vertex, the
+    // correction the velocity sampler adds near open tilts; filled once per step before the
+    // advection (k_tilt_corr) so the samplers read it instead of sampling the MAC grid again
+    const double* corrT;
 };
 
 ASTG_HD inline void report(const Dev& d, int code) {

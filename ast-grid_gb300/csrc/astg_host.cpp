@@ -1053,13 +1053,19 @@ struct astg_handle {
                 if (d.sdf) launch_collider_dual(d, C, st);
                 launch_dual_ghost(d, C, st);
                 break;
-            case 5:
-                if (P.tilt_adaptivity) launch_adjust(d, C, N, dOpen, dFixed, dt, st);
-                launch_advect_scalars(d, C, N, dOpen, dt, st);
-                launch_advect_velocity(d, C, N, dt, st);
+            case 5: {
+                // the velocity is final for this step: its tilt corrections once, read by every sample
+                if (!dCorrT) dCorrT = dalloc<double>((size_t)3 * S);
+                Fields Cc = C;
+                Cc.corrT = dCorrT;
+                launch_tilt_corr(d, Cc, dCorrT, st);
+                if (P.tilt_adaptivity) launch_adjust(d, Cc, N, dOpen, dFixed, dt, st);
+                launch_advect_scalars(d, Cc, N, dOpen, dt, st);
+                launch_advect_velocity(d, Cc, N, dt, st);
                 cur = 1 - cur;
                 launch_decay(d, F[cur], st);
                 break;
+            }
             default: throw std::invalid_argument("stage must be 0..5");
         }
         ck(cudaGetLastError(), "launch");
@@ -1285,6 +1291,7 @@ struct astg_handle {
     uint16_t* dColMask = nullptr;
     int* dHalfDir = nullptr;
     double* dMacBefore = nullptr;
+    double* dCorrT = nullptr;  // tilt corrections of the current velocity (stage 5)
     void setCollider(const double* sdf, size_t bytes) {
         size_t n = (size_t)res * res * res;
         if (bytes == 0) {

@@ -209,6 +209,8 @@ void launch_collider_mac(const Dev& d, const Fields& F, double* before, cudaStre
 void launch_collider_tilt(const Dev& d, const Fields& F, cudaStream_t st);
 void launch_collider_dual(const Dev& d, const Fields& F, cudaStream_t st);
 void launch_walls(const Dev& d, double* mac, cudaStream_t st);
+// Fields::corrT for the velocity F (3 * S doubles)
+void launch_tilt_corr(const Dev& d, const Fields& F, double* corr, cudaStream_t st);
 void launch_dual_update(const Dev& d, const Fields& F, cudaStream_t st);
 void launch_force(const Dev& d, const Fields& F, const uint8_t* open, const double* amb, double dt, cudaStream_t st);
 void launch_walls_and_ghost(const Dev& d, const Fields& F, const uint8_t* lastWriter, cudaStream_t st);

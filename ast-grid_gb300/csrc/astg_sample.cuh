@@ -212,12 +212,14 @@ ASTG_HD inline double mac_axis(const Dev& d, int a, int l, double rx, double ry,
                            U[req(d, l, id[0], id[1], id1[2])], U[req(d, l, id1[0], id[1], id1[2])],
                            U[req(d, l, id[0], id1[1], id1[2])], U[req(d, l, id1[0], id1[1], id1[2])], f[0], f[1], f[2]);
 }
-ASTG_HD inline V3 mac_sample(const Dev& d, V3 p, const double* mac) {
-    int l = level_of(d, p.x, p.y, p.z);
-    double h = d.ldh[l];
-    double rx = over_h(d, p.x, l), ry = over_h(d, p.y, l), rz = over_h(d, p.z, l);
+// the MAC grid's velocity at level l, (rx, ry, rz) = p / dx_l
+ASTG_HD inline V3 mac_sample_at(const Dev& d, int l, double rx, double ry, double rz, const double* mac) {
     return v3(mac_axis(d, 0, l, rx, ry, rz, mac), mac_axis(d, 1, l, rx, ry, rz, mac + d.S),
               mac_axis(d, 2, l, rx, ry, rz, mac + 2 * (size_t)d.S));
+}
+ASTG_HD inline V3 mac_sample(const Dev& d, V3 p, const double* mac) {
+    int l = level_of(d, p.x, p.y, p.z);
+    return mac_sample_at(d, l, over_h(d, p.x, l), over_h(d, p.y, l), over_h(d, p.z, l), mac);
 }
 ASTG_HD inline double mac_sample_one(const Dev& d, int a, V3 p, const double* mac) {
     int l = level_of(d, p.x, p.y, p.z);
@@ -225,23 +227,62 @@ ASTG_HD inline double mac_sample_one(const Dev& d, int a, V3 p, const double* ma
     return mac_axis(d, a, l, over_h(d, p.x, l), over_h(d, p.y, l), over_h(d, p.z, l), mac + (size_t)a * d.S);
 }
 
+// one component of the dual vectors
+struct CompAt {
+    const double* p;
+    int a;
+    ASTG_HD double operator()(int s) const { return p[3 * s + a]; }
+};
+// the correction of the tilt at slot ts: its dual vector minus the MAC velocity at its vertex
+ASTG_HD inline V3 tilt_corr(const Dev& d, int ts, const Fields& F) {
+    if (F.corrT) return v3(F.corrT[3 * ts], F.corrT[3 * ts + 1], F.corrT[3 * ts + 2]);
+    V3 dt = v3(F.dualT[3 * ts], F.dualT[3 * ts + 1], F.dualT[3 * ts + 2]);
+    return dt - mac_sample(d, vert_pos(d, ts), F.mac);
+}
+
 // OctreeOmniFaceCenteredGrid3::sample, include/octree_omni_face_centered_grid3.h:37-80
 ASTG_HD inline V3 vel_sample(const Dev& d, V3 p, const Fields& F) {
     int l = level_of(d, p.x, p.y, p.z);
-    double h = d.ldh[l];
     int r = d.lres[l];
+    const double rx = over_h(d, p.x, l), ry = over_h(d, p.y, l), rz = over_h(d, p.z, l);
     int id0, id1, id2;
     double f0, f1, f2;
-    bary_vec(over_h(d, p.x, l) - 0.5, r - 1, &id0, &f0);
-    bary_vec(over_h(d, p.y, l) - 0.5, r - 1, &id1, &f1);
-    bary_vec(over_h(d, p.z, l) - 0.5, r - 1, &id2, &f2);
+    bary_vec(rx - 0.5, r - 1, &id0, &f0);
+    bary_vec(ry - 0.5, r - 1, &id1, &f1);
+    bary_vec(rz - 0.5, r - 1, &id2, &f2);
     int ts = req(d, l, id0 + 1, id1 + 1, id2 + 1);
     if (near_transition(d, l, id0, id1, id2)) return omni_sample_sub<V3>(d, p, Vec3At{F.dualO}, Vec3At{F.dualT}, F.tf);
-    V3 v = mac_sample(d, p, F.mac);
+    V3 v = mac_sample_at(d, l, rx, ry, rz, F.mac);
     uint32_t tn = F.tf[ts];
     if (!(tn & TF_HALF) && (tn & TF_CLOSED)) return v;
-    V3 dt = v3(F.dualT[3 * ts], F.dualT[3 * ts + 1], F.dualT[3 * ts + 2]);
-    V3 diff = dt - mac_sample(d, vert_pos(d, ts), F.mac);
+    V3 diff = tilt_corr(d, ts, F);
+    double mn = dmin(dmin(dmin(f0, f1), f2), dmin(dmin(1 - f0, 1 - f1), 1 - f2));
+    return v + diff * 2 * mn;
+}
+// component a of vel_sample: every component is computed on its own (the same operations on the
+// same values), so this is vel_sample(d, p, F)'s component a bit for bit at a third of the MAC work
+ASTG_HD inline double vel_sample_axis(const Dev& d, V3 p, const Fields& F, int a) {
+    int l = level_of(d, p.x, p.y, p.z);
+    int r = d.lres[l];
+    const double rx = over_h(d, p.x, l), ry = over_h(d, p.y, l), rz = over_h(d, p.z, l);
+    int id0, id1, id2;
+    double f0, f1, f2;
+    bary_vec(rx - 0.5, r - 1, &id0, &f0);
+    bary_vec(ry - 0.5, r - 1, &id1, &f1);
+    bary_vec(rz - 0.5, r - 1, &id2, &f2);
+    int ts = req(d, l, id0 + 1, id1 + 1, id2 + 1);
+    if (near_transition(d, l, id0, id1, id2))
+        return omni_sample_sub<double>(d, p, CompAt{F.dualO, a}, CompAt{F.dualT, a}, F.tf);
+    double v = mac_axis(d, a, l, rx, ry, rz, F.mac + (size_t)a * d.S);
+    uint32_t tn = F.tf[ts];
+    if (!(tn & TF_HALF) && (tn & TF_CLOSED)) return v;
+    double diff;
+    if (F.corrT) {
+        diff = F.corrT[3 * ts + a];
+    } else {
+        V3 q = vert_pos(d, ts);
+        diff = F.dualT[3 * ts + a] - mac_sample_one(d, a, q, F.mac);
+    }
     double mn = dmin(dmin(dmin(f0, f1), f2), dmin(dmin(1 - f0, 1 - f1), 1 - f2));
     return v + diff * 2 * mn;
 }

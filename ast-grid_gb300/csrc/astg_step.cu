@@ -622,7 +622,7 @@ __global__ void k_adv_mac(Dev d, Fields cur, Fields nxt, double dt) {
     int a = (int)(idx / d.S), s = (int)(idx - (long long)a * d.S);
     if (ghost(d, s)) return;
     V3 o = back_trace(d, mac_pos(d, a, s), dt, cur);
-    nxt.mac[(size_t)a * d.S + s] = comp(vel_sample(d, o, cur), a);
+    nxt.mac[(size_t)a * d.S + s] = vel_sample_axis(d, o, cur, a);
 }
 // one thread per (tilt, slot)
 __global__ void k_adv_tilt(Dev d, Fields cur, Fields nxt, double dt) {
@@ -668,6 +668,18 @@ void launch_advect_scalars(const Dev& d, const Fields& cur, const Fields& nxt, c
     if (d.H) ASTG_LAUNCH(k_adv_scalar_half<<<nblk(d.H), TB, 0, st>>>(d, cur, nxt, dt));
     launch_scalar_ghost(d, nxt.dO, nxt.dT, nxt.te, nxt.tf, st);
     launch_scalar_ghost(d, nxt.hO, nxt.hT, nxt.te, nxt.tf, st);
+}
+// the dual-grid correction of every tilt for the current velocity (see Fields::corrT)
+__global__ void k_tilt_corr(Dev d, Fields F, double* corr) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.S) return;
+    V3 m = mac_sample(d, vert_pos(d, s), F.mac);
+    corr[3 * s] = F.dualT[3 * s] - m.x;
+    corr[3 * s + 1] = F.dualT[3 * s + 1] - m.y;
+    corr[3 * s + 2] = F.dualT[3 * s + 2] - m.z;
+}
+void launch_tilt_corr(const Dev& d, const Fields& F, double* corr, cudaStream_t st) {
+    ASTG_LAUNCH(k_tilt_corr<<<nblk(d.S), TB, 0, st>>>(d, F, corr));
 }
 void launch_advect_velocity(const Dev& d, const Fields& cur, const Fields& nxt, double dt, cudaStream_t st) {
     ASTG_LAUNCH(k_adv_mac<<<nblk(3LL * d.S), TB, 0, st>>>(d, cur, nxt, dt));
