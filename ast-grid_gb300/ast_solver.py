@@ -26,7 +26,7 @@ FP64, MIXED = 0, 1
 
 # exported symbols of include/astg.h
 SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_update",
-           "astg_set_max_cfl", "astg_cfl", "astg_stage", "astg_refine_split_map",
+           "astg_set_max_cfl", "astg_cfl", "astg_stage", "astg_refine_split_map", "astg_set_collider_sphere",
            "astg_set_solver_parameters", "astg_set_precision", "astg_set_reduction_order", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
            "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate",
            "astg_restart", "astg_save_checkpoint", "astg_tape_start", "astg_tape_stop", "astg_adjoint_reset",
@@ -102,6 +102,7 @@ def lib(path=None):
         L.astg_set_precision.argtypes = [c_p, ctypes.c_int]
         L.astg_update.argtypes = [c_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(StepStats)]
         L.astg_set_max_cfl.argtypes = [c_p, ctypes.c_double]
+        L.astg_set_collider_sphere.argtypes = [c_p, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.astg_refine_split_map.argtypes = [c_p, ctypes.c_int, ctypes.c_int, c_p, ctypes.c_double, ctypes.c_double]
         L.astg_cfl.argtypes = [c_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.astg_set_reduction_order.argtypes = [c_p, ctypes.c_int, ctypes.c_int]
@@ -337,6 +338,12 @@ class OctreeSmoke3:
     def set(self, name, arr):
         a = np.ascontiguousarray(arr, dtype=_dtype(name)).ravel()
         self._check(lib().astg_set(self._h, name.encode(), a.ctypes.data, a.nbytes))
+
+    def set_collider_sphere(self, center=(0.5, 0.5, 0.45), radius=0.1):
+        """OmniBoundarySolver3::updateCollider with a Sphere3 (the stock obstacle by default); the SDF
+        grid is computed on the device.  radius <= 0 removes the collider."""
+        cx, cy, cz = (float(v) for v in center)
+        self._check(lib().astg_set_collider_sphere(self._h, cx, cy, cz, float(radius)))
 
     # torch tensors: the library copies straight from / into device (or host) memory
     def get_tensor(self, name, device="cuda"):

@@ -182,6 +182,43 @@ __global__ void k_col_dual(Dev d, Fields F) {
     F.dualT[3 * s + 2] = t.z;
 }
 
+// OmniBoundarySolver3::updateCollider (src/omni_boundary_solver3.cpp:17-32) for a Sphere3 collider
+// wrapped in ShapeToImplicit3 (the stock obstacle, src/octree_omnigrid_solver3.cpp:157-158): the
+// signed distance of ShapeToImplicit3::signedDistanceLocal (include/geometry/shape_to_implicit3.h:41-46)
+// at each finest cell centre (i + 0.5) * dx.  Both transforms have identity orientations, so toLocal
+// and toWorld are exact translations; the closest point is the centre plus the radius times the
+// normalised offset, (1, 0, 0) when the offset's norm is below epsilon (include/geometry/sphere3.h:20-26).
+// Norms and the dot product of these plain 3-vectors are Eigen's packet reductions: the first two
+// terms as one SSE2 packet, then the third, (t0 + t1) + t2 (Eigen/src/Core/Redux.h:306-329).
+__device__ __forceinline__ double sq3p(V3 n) { return (n.x * n.x + n.y * n.y) + n.z * n.z; }
+__global__ void k_col_sphere_sdf(int res, double dx, double cx, double cy, double cz, double r, double* sdf) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = (long long)res * res * res;
+    if (i >= n) return;
+    const int x = (int)(i % res), y = (int)((i / res) % res), z = (int)(i / ((long long)res * res));
+    const V3 p = v3((x + 0.5) * dx, (y + 0.5) * dx, (z + 0.5) * dx);
+    const V3 c = v3(cx, cy, cz);
+    const V3 q = p - c;
+    V3 nl = v3(1, 0, 0);
+    if (!(sqrt(sq3p(q)) < EPS)) {
+        double zz = sq3p(q);
+        nl = q;
+        if (zz > 0) {
+            double k = sqrt(zz);
+            nl = v3(q.x / k, q.y / k, q.z / k);
+        }
+    }
+    const V3 xc = v3(nl.x * r, nl.y * r, nl.z * r) + c;
+    const V3 off = p - xc;
+    const double dot = (nl.x * off.x + nl.y * off.y) + nl.z * off.z;
+    const double len = sqrt(sq3p(xc - p));
+    sdf[i] = dot < 0.0 ? -len : len;
+}
+void launch_collider_sphere_sdf(int res, double cx, double cy, double cz, double r, double* sdf, cudaStream_t st) {
+    const long long n = (long long)res * res * res;
+    ASTG_LAUNCH(k_col_sphere_sdf<<<(unsigned)((n + CTB - 1) / CTB), CTB, 0, st>>>(res, 1.0 / res, cx, cy, cz, r, sdf));
+}
+
 // halfDir: each half tilt's direction (0-5, the list order of d.half)
 void launch_collider_setup(const Dev& d, const int* halfDir, uint16_t* mask, double* wMac, double* wTilt,
                            cudaStream_t st) {

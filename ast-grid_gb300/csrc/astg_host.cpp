@@ -1284,7 +1284,8 @@ struct astg_handle {
     // ---------------------------------------------------------------- collider
     // OmniBoundarySolver3::updateCollider (src/omni_boundary_solver3.cpp:17-32) takes a shape and
     // samples its SDF at the finest cell centres; here the caller passes that grid (res^3 doubles,
-    // index (z * res + y) * res + x), or nothing to remove the collider.  The cut-cell weights
+    // index (z * res + y) * res + x) or a sphere whose grid is computed on the device (the stock
+    // obstacle), or nothing to remove the collider.  The cut-cell weights
     // (initCuttingCellWeights, which initialize() runs right after initObstacle) are recomputed on
     // the device and copied back so astg_get("w_mac" / "w_tilt") returns them.
     double* dSdf = nullptr;
@@ -1305,6 +1306,23 @@ struct astg_handle {
         }
         if (bytes != 8 * n) throw std::invalid_argument("astg_set collider_sdf: expected res^3 doubles (" + std::to_string(8 * n) + " bytes)");
         if (T.on) throw std::invalid_argument("astg_set collider_sdf: a tape is active");
+        allocCollider();
+        up(dSdf, sdf, n);
+        colliderFromSdf();
+    }
+    // the stock obstacle: a sphere's SDF grid computed on the device (radius <= 0 removes the collider)
+    void setColliderSphere(double cx, double cy, double cz, double r) {
+        if (!(r > 0)) {
+            setCollider(nullptr, 0);
+            return;
+        }
+        if (T.on) throw std::invalid_argument("astg_set_collider_sphere: a tape is active");
+        allocCollider();
+        launch_collider_sphere_sdf(res, cx, cy, cz, r, dSdf, st);
+        colliderFromSdf();
+    }
+    void allocCollider() {
+        size_t n = (size_t)res * res * res;
         if (!dSdf) {
             dSdf = dalloc<double>(n);
             dColMask = dalloc<uint16_t>(S);
@@ -1313,7 +1331,9 @@ struct astg_handle {
             for (int i = 0; i < H; ++i) dirs[i] = te[0][half[i]].dir;
             dHalfDir = upload(dirs);
         }
-        up(dSdf, sdf, n);
+    }
+    // the cut-cell weights and solid masks of the SDF grid in dSdf
+    void colliderFromSdf() {
         d.sdf = dSdf;
         d.colMask = dColMask;
         launch_collider_setup(d, dHalfDir, dColMask, const_cast<double*>(d.wMac), const_cast<double*>(d.wTilt), st);
@@ -1694,6 +1714,12 @@ struct astg_handle {
         if (name == "w_mac") { size_t nb = need(8 * wMac.size()); if (dst) memcpy(dst, wMac.data(), nb); return nb; }
         if (name == "w_tilt") { size_t nb = need(8 * wTilt.size()); if (dst) memcpy(dst, wTilt.data(), nb); return nb; }
         if (name == "dual_tables") { size_t nb = need(8 * M37.size()); if (dst) memcpy(dst, M37.data(), nb); return nb; }
+        if (name == "collider_sdf") {
+            size_t n = d.sdf ? (size_t)res * res * res : 0;
+            size_t nb = need(8 * n);
+            if (dst && n) down(dSdf, dst, n);
+            return nb;
+        }
         if (name == "pindex_oct") { size_t nb = need(4 * (size_t)S); if (dst) down(J.pO, dst, S); return nb; }
         if (name == "pindex_tilt") { size_t nb = need(4 * (size_t)S); if (dst) down(J.pT, dst, S); return nb; }
         if (name == "A_rowptr") { int n = lastN(); size_t nb = need(4 * (size_t)(n + 1)); if (dst) down(J.rowPtr, dst, n + 1); return nb; }
@@ -1962,6 +1988,11 @@ astg_status astg_update(astg_handle* h, double dt, int* substeps, astg_step_stat
     astg_status s = guard(h, [&] { h->update(dt, substeps, stats); });
     if (s == ASTG_OK && !h->updateConverged) return ASTG_NOT_CONVERGED;
     return s;
+}
+
+astg_status astg_set_collider_sphere(astg_handle* h, double cx, double cy, double cz, double radius) {
+    if (!h || !std::isfinite(cx) || !std::isfinite(cy) || !std::isfinite(cz) || std::isnan(radius)) return ASTG_BAD_ARG;
+    return guard(h, [&] { h->setColliderSphere(cx, cy, cz, radius); });
 }
 
 astg_status astg_set_max_cfl(astg_handle* h, double max_cfl) {

@@ -202,6 +202,8 @@ void launch_mean_temperature_ref(const Dev& d, const double* hO, int workers, do
 void launch_max_face(const Dev& d, const double* mac, unsigned long long* out, cudaStream_t st);
 // collider (astg_collider.cu): per-slot bits and cut-cell weights once per collider; the per-step
 // wipe and inside-solid constraints (before: 3 * S doubles of scratch for the MAC projection)
+// the SDF grid of a sphere collider at the finest cell centres (res^3 doubles)
+void launch_collider_sphere_sdf(int res, double cx, double cy, double cz, double r, double* sdf, cudaStream_t st);
 void launch_collider_setup(const Dev& d, const int* halfDir, uint16_t* mask, double* wMac, double* wTilt,
                            cudaStream_t st);
 void launch_collider_wipe(const Dev& d, const Fields& F, cudaStream_t st);

@@ -111,6 +111,14 @@ astg_status astg_step(astg_handle* h, double dt, astg_step_stats* stats);
  * the frame.  ASTG_NOT_CONVERGED when any sub-step's solve did not converge. */
 astg_status astg_update(astg_handle* h, double dt, int* substeps, astg_step_stats* stats);
 
+/* OmniBoundarySolver3::updateCollider (src/omni_boundary_solver3.cpp:17-32) with a Sphere3 collider
+ * of radius `radius` centred at (cx, cy, cz), as OctreeOmniGridSolver3::initObstacle builds the stock
+ * one ((0.5, 0.5, 0.45), 0.1; src/octree_omnigrid_solver3.cpp:150-158): the SDF grid is computed on
+ * the device at the finest cell centres, then the cut-cell weights and solid masks as for astg_set
+ * "collider_sdf".  radius <= 0 removes the collider.  The inside-solid projection keeps taking its
+ * normals from "collider_centre" (the reference hard-codes it, whatever the collider). */
+astg_status astg_set_collider_sphere(astg_handle* h, double cx, double cy, double cz, double radius);
+
 /* setMaxCfl (include/octree_omnigrid_solver3.h:29); the default is the reference's 3. */
 astg_status astg_set_max_cfl(astg_handle* h, double max_cfl);
 
@@ -166,9 +174,10 @@ long long astg_size(const astg_handle* h, int what);
  *   5 half tilt; half direction)  tilt_open (u8, slots: bit 0 open, bit 1 fixed)
  *   source_density_oct source_density_tilt (f64, slots: density the source sets, default 1)
  *   prefix "t_" = the swap-partner buffer of the reference's double-buffered grids;
- * write only: collider_sdf (f64, res^3 at the finest cell centres, index (z * res + y) * res + x:
- *   OmniBoundarySolver3::updateCollider's SDF grid, inside negative; 0 bytes removes the collider;
- *   the cut-cell weights are recomputed) and collider_centre (f64 x 3: the centre the inside-solid
+ * collider_sdf (f64, res^3 at the finest cell centres, index (z * res + y) * res + x:
+ *   OmniBoundarySolver3::updateCollider's SDF grid, inside negative; 0 bytes without a collider;
+ *   set: 0 bytes removes the collider, else the cut-cell weights are recomputed);
+ * write only: collider_centre (f64 x 3: the centre the inside-solid
  *   projection takes its normals from, the reference's hard-coded (0.5, 0.5, 0.45) by default);
  * read only: slot_coords (i32, slots x 4: x y z flags) level_sizes (i32, levels x 3)
  *   half_tilts t_joints closed_by_half_tilt (i64 packed level coordinates) split_map (i32)

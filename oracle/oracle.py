@@ -22,7 +22,7 @@ SRC2D = os.path.join(HERE, "ast2d_oracle.cpp")
 
 # array names and element types exposed by orc_get
 F64 = {"density_oct", "density_tilt", "heat_oct", "heat_tilt", "mac", "tilt_vel", "dual_oct", "dual_tilt",
-       "tilt_e", "w_mac", "w_tilt", "A_val", "b", "p", "pcg_err", "ambT", "dual_tables"}
+       "tilt_e", "w_mac", "w_tilt", "A_val", "b", "p", "pcg_err", "ambT", "dual_tables", "collider_sdf"}
 I32 = {"tilt_flags", "slot_coords", "level_sizes", "split_map", "pindex_oct", "pindex_tilt", "A_rowptr",
        "A_col", "pcg_iters", "anomalies"}
 I64 = {"half_tilts", "t_joints", "closed_by_half_tilt"}

@@ -809,6 +809,42 @@ public:
     // norm when it is positive, Eigen/src/Core/Dot.h:145-151)
     static double sq3(const V3& n) { return n.x * n.x + (n.y * n.y + n.z * n.z); }
     static double norm3(const V3& n) { return std::sqrt(sq3(n)); }
+    // OmniBoundarySolver3::updateCollider (src/omni_boundary_solver3.cpp:17-32) for a Sphere3 in
+    // ShapeToImplicit3: signedDistanceLocal (include/geometry/shape_to_implicit3.h:41-46) at each
+    // cell centre (i + 0.5) * dx of the finest grid.  Sphere3::closestNormalLocal
+    // (include/geometry/sphere3.h:24-26) is (1, 0, 0) below epsilon, else normalized(); the
+    // transforms' identity orientations leave translations only.  These norms and the dot product
+    // are on plain 3-vectors, which Eigen reduces with one SSE2 packet for the first two terms and
+    // the third added after, (t0 + t1) + t2 (Eigen/src/Core/Redux.h:306-329).
+    static double sq3p(const V3& n) { return (n.x * n.x + n.y * n.y) + n.z * n.z; }
+    void sphereSdf(const V3& c, double r) {
+        if (!(r > 0)) {
+            colSdf.clear();
+            return;
+        }
+        const double dx = 1.0 / res;
+        colSdf.assign((size_t)res * res * res, 0.0);
+        for (int z = 0; z < res; ++z)
+            for (int y = 0; y < res; ++y)
+                for (int x = 0; x < res; ++x) {
+                    V3 p = v3((x + 0.5) * dx, (y + 0.5) * dx, (z + 0.5) * dx);
+                    V3 q = p - c;
+                    V3 nl = v3(1, 0, 0);
+                    if (!(std::sqrt(sq3p(q)) < DBL_EPSILON)) {
+                        double zz = sq3p(q);
+                        nl = q;
+                        if (zz > 0) {
+                            double k = std::sqrt(zz);
+                            nl = v3(q.x / k, q.y / k, q.z / k);
+                        }
+                    }
+                    V3 xc = v3(nl.x * r, nl.y * r, nl.z * r) + c;
+                    V3 off = p - xc;
+                    double dot = (nl.x * off.x + nl.y * off.y) + nl.z * off.z;
+                    double len = std::sqrt(sq3p(xc - p));
+                    colSdf[((size_t)z * res + y) * res + x] = dot < 0.0 ? -len : len;
+                }
+    }
     static V3 tangential(const V3& v, V3 n) {
         double z = sq3(n);
         if (z > 0) {
@@ -2473,6 +2509,7 @@ long long orc_get(void* h, const char* name, void* buf, long long cap) {
         return outd(v);
     }
     if (n == "w_tilt") return outd(s->wTilt);
+    if (n == "collider_sdf") return outd(s->colSdf);
     if (n == "pindex_oct") return outi(s->pO);
     if (n == "pindex_tilt") return outi(s->pT);
     if (n == "A_rowptr") return outi(s->csrPtr);
@@ -2500,6 +2537,13 @@ int orc_set(void* h, const char* name, const void* buf, long long count) {
         long long r = s->res;
         if (count != 0 && count != r * r * r) return 1;
         s->colSdf.assign((const double*)buf, (const double*)buf + count);
+        s->cuttingCellWeights();
+        return 0;
+    }
+    if (n == "collider_sphere") {  // cx cy cz r: the SDF grid of a sphere collider (r <= 0: none)
+        if (count != 4) return 1;
+        const double* q = (const double*)buf;
+        s->sphereSdf(oracle::v3(q[0], q[1], q[2]), q[3]);
         s->cuttingCellWeights();
         return 0;
     }

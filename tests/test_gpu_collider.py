@@ -110,3 +110,45 @@ def test_removing_the_collider_restores_the_free_domain():
         s.set("collider_sdf", np.zeros(7))
     s.close()
     free.close()
+
+
+def test_sphere_collider_on_device_bit_identical_to_reference():
+    """astg_set_collider_sphere: the stock obstacle's SDF grid computed on the device equals the
+    reference's grid; the weights and four steps then match the reference bit for bit as with the
+    grid passed in.  radius 0 removes the collider."""
+    import ast_solver
+
+    name = "ref_col_c8_l3"
+    g = golden(name)
+    c, lv, steps = case(name)
+    s = ast_solver.OctreeSmoke3(c, lv)
+    s.set_reduction_order("reference", 8)
+    s.set_collider_sphere((0.5, 0.5, 0.45), 0.1)
+    assert_same("collider_sdf", g["collider_sdf"].ravel(), s.get("collider_sdf"))
+    for k in ["w_mac", "w_tilt"]:
+        assert_same(k, g[k], s.get(k))
+    for k in range(1, steps + 1):
+        s.update(DT)
+        st = state(g, f"step{k}/")
+        for f in FIELDS + ["tilt_open", "p"]:
+            assert_same(f"step{k}/{f}", st[f], s.get(f))
+    s.set_collider_sphere((0.5, 0.5, 0.45), 0.0)
+    assert s.get("collider_sdf").size == 0
+    free = ast_solver.OctreeSmoke3(c, lv)
+    assert_same("w_mac", free.get("w_mac"), s.get("w_mac"))
+    s.close()
+    free.close()
+
+
+def test_sphere_collider_sdf_at_full_resolution():
+    """At 64^3 coarsest x 3 levels (res 256) the device grid equals the oracle's restatement, which
+    is pinned to the reference's grid at res 32 and 64."""
+    import ast_solver
+    from oracle.oracle import Oracle
+
+    s = ast_solver.OctreeSmoke3(64, 3)
+    s.set_collider_sphere((0.5, 0.5, 0.45), 0.1)
+    o = Oracle(64, 3)
+    o.set("collider_sphere", [0.5, 0.5, 0.45, 0.1])
+    assert_same("collider_sdf", o.get("collider_sdf"), s.get("collider_sdf"))
+    s.close()

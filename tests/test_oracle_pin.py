@@ -214,3 +214,20 @@ def test_collider_racy_case_close_to_reference():
         assert max_rel(st["p"], o.get("p")) <= 3e-3
         for f in ["density_oct", "density_tilt", "heat_oct", "heat_tilt"]:
             assert max_rel(st[f], o.get(f)) <= 1e-5, f
+
+
+@pytest.mark.parametrize("name", ["ref_col_c8_l3", "ref_refine_c16_l3"])
+def test_sphere_collider_sdf_bit_exact(name):
+    """OmniBoundarySolver3::updateCollider's SDF grid of the stock sphere (r = 0.1 at (0.5, 0.5, 0.45),
+    through ShapeToImplicit3::signedDistanceLocal) computed by the oracle equals the grid the
+    reference filled, at res 32 and 64; the cut-cell weights follow from it unchanged."""
+    g = golden(name)
+    c, lv = g["meta/case"].tolist()[:2]
+    o = Oracle(c, lv)
+    o.set("collider_sphere", [0.5, 0.5, 0.45, 0.1])
+    assert_same("collider_sdf", g["collider_sdf"].ravel(), o.get("collider_sdf"))
+    if "w_mac" in g:
+        for k in ["w_mac", "w_tilt"]:
+            assert_same(k, g[k], o.get(k))
+    o.set("collider_sphere", [0.5, 0.5, 0.45, 0.0])
+    assert o.get("collider_sdf").size == 0
