@@ -113,9 +113,11 @@ ASTG_HD void neighbor_cube(const Dev& d, int l, int xi, int yi, int zi, int dir,
     }
 }
 
-// OctreeOmniGrid3<T>::sampleSub, include/octree_omni_grid3.h:243-286
+// OctreeOmniGrid3<T>::sampleSub, include/octree_omni_grid3.h:243-286.  Out of line: it runs only
+// near level transitions, and inlining it at every sample site multiplies the samplers' code size
+// (instruction-cache misses were the largest stall of the advection kernels)
 template <class T, class GO, class GT>
-ASTG_HD T omni_sample_sub(const Dev& d, V3 p, const GO& oct, const GT& til, const uint32_t* tf) {
+__device__ __noinline__ T omni_sample_sub(const Dev& d, V3 p, const GO& oct, const GT& til, const uint32_t* tf) {
     int l = level_of(d, p.x, p.y, p.z);
     double h = d.ldh[l];
     int r = d.lres[l];
@@ -168,10 +170,13 @@ ASTG_HD inline bool near_transition(const Dev& d, int l, int xi, int yi, int zi)
     return false;
 }
 
-// OctreeOmniGrid3<double>::sample, correction-based, include/octree_omni_grid3.h:147-187
-ASTG_HD inline double scalar_sample(const Dev& d, V3 p, const double* oct, const double* til, const uint32_t* tf) {
+// OctreeOmniGrid3<double>::sample, correction-based, include/octree_omni_grid3.h:147-187, for one or
+// two fields at the same point (density and heat): the point is located once; each value takes the
+// same operations on the same inputs as a sample of its field alone
+template <int NF>
+ASTG_HD inline void scalar_sample_n(const Dev& d, V3 p, const double* const* oct, const double* const* til,
+                                    const uint32_t* tf, double* out) {
     int l = level_of(d, p.x, p.y, p.z);
-    double h = d.ldh[l];
     int r = d.lres[l];
     int xi, yi, zi;
     double fx, fy, fz;
@@ -180,16 +185,44 @@ ASTG_HD inline double scalar_sample(const Dev& d, V3 p, const double* oct, const
     bary(over_h(d, p.z, l) - 0.5, 0, r - 2, &zi, &fz);
     int x1 = imin(xi + 1, r - 2), y1 = imin(yi + 1, r - 2), z1 = imin(zi + 1, r - 2);
     int ts = req(d, l, xi + 1, yi + 1, zi + 1);
-    if (near_transition(d, l, xi, yi, zi)) return omni_sample_sub<double>(d, p, ScalarAt{oct}, ScalarAt{til}, tf);
-    double o000 = oct[req(d, l, xi, yi, zi)], o100 = oct[req(d, l, x1, yi, zi)], o010 = oct[req(d, l, xi, y1, zi)],
-           o110 = oct[req(d, l, x1, y1, zi)], o001 = oct[req(d, l, xi, yi, z1)], o101 = oct[req(d, l, x1, yi, z1)],
-           o011 = oct[req(d, l, xi, y1, z1)], o111 = oct[req(d, l, x1, y1, z1)];
-    double ret = trilerp<double>(o000, o100, o010, o110, o001, o101, o011, o111, fx, fy, fz);
-    uint32_t tn = tf[ts];
-    if ((tn & TF_CLOSED) && !(tn & TF_HALF)) return ret;
-    double diff = til[ts] - (1 / 8.0) * (o000 + o100 + o010 + o110 + o001 + o101 + o011 + o111);
-    double mn = dmin(dmin(dmin(fx, fy), fz), dmin(dmin(1 - fx, 1 - fy), 1 - fz));
-    return ret + diff * 2.0 * mn;
+    if (near_transition(d, l, xi, yi, zi)) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) out[f] = omni_sample_sub<double>(d, p, ScalarAt{oct[f]}, ScalarAt{til[f]}, tf);
+        return;
+    }
+    const int s000 = req(d, l, xi, yi, zi), s100 = req(d, l, x1, yi, zi), s010 = req(d, l, xi, y1, zi),
+              s110 = req(d, l, x1, y1, zi), s001 = req(d, l, xi, yi, z1), s101 = req(d, l, x1, yi, z1),
+              s011 = req(d, l, xi, y1, z1), s111 = req(d, l, x1, y1, z1);
+    const uint32_t tn = tf[ts];
+    const bool plain = (tn & TF_CLOSED) && !(tn & TF_HALF);
+    const double mn = dmin(dmin(dmin(fx, fy), fz), dmin(dmin(1 - fx, 1 - fy), 1 - fz));
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        const double* o = oct[f];
+        double o000 = o[s000], o100 = o[s100], o010 = o[s010], o110 = o[s110], o001 = o[s001], o101 = o[s101],
+               o011 = o[s011], o111 = o[s111];
+        double ret = trilerp<double>(o000, o100, o010, o110, o001, o101, o011, o111, fx, fy, fz);
+        if (!plain) {
+            double diff = til[f][ts] - (1 / 8.0) * (o000 + o100 + o010 + o110 + o001 + o101 + o011 + o111);
+            ret = ret + diff * 2.0 * mn;
+        }
+        out[f] = ret;
+    }
+}
+ASTG_HD inline double scalar_sample(const Dev& d, V3 p, const double* oct, const double* til, const uint32_t* tf) {
+    double v;
+    scalar_sample_n<1>(d, p, &oct, &til, tf, &v);
+    return v;
+}
+// density and heat at one point
+ASTG_HD inline void scalar_sample2(const Dev& d, V3 p, const double* o0, const double* t0, const double* o1,
+                                   const double* t1, const uint32_t* tf, double* v0, double* v1) {
+    const double* o[2] = {o0, o1};
+    const double* t[2] = {t0, t1};
+    double v[2];
+    scalar_sample_n<2>(d, p, o, t, tf, v);
+    *v0 = v[0];
+    *v1 = v[1];
 }
 
 // OctreeFaceCenteredGrid3::sampleX/Y/Z, src/octree_face_centered_grid3.cpp:36-121
@@ -313,8 +346,14 @@ ASTG_HD inline double bsdf(const Dev& d, V3 p) { return d.sdf ? sdf_sample(d.sdf
 // sign between p and the traced point, the point moves back toward p by |phi1| / (|phi0| + |phi1|)
 // (never without a collider: the SDF is 1 everywhere)
 ASTG_HD inline V3 back_trace(const Dev& d, V3 p, double dt, const Fields& F) {
-    V3 mid = p - vel_sample(d, p, F) * dt * 0.5;
-    V3 ret = p - vel_sample(d, mid, F) * dt;
+    // mid = p - v(p) dt / 2, ret = p - v(mid) dt; a loop, so the sampler's code is emitted once
+    V3 q = p, ret = p;
+#pragma unroll 1
+    for (int i = 0; i < 2; ++i) {
+        V3 v = vel_sample(d, q, F) * dt;
+        if (i == 0) q = p - v * 0.5;
+        else ret = p - v;
+    }
     if (d.sdf) {
         double phi0 = bsdf(d, p), phi1 = bsdf(d, ret);
         if (phi0 * phi1 < 0.0) {

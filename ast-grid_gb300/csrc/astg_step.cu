@@ -193,7 +193,9 @@ void launch_source(const Dev& d, const Fields& F, cudaStream_t st) {
 // ------------------------------------------------------------------ buoyancy
 // src/octree_omnigrid_solver3.cpp:917-972; amb points at the device mean temperature
 ASTG_HD inline double force_at(const Dev& d, const Fields& F, V3 p, double amb) {
-    return d.buoyD * scalar_sample(d, p, F.dO, F.dT, F.tf) + d.buoyT * (scalar_sample(d, p, F.hO, F.hT, F.tf) - amb);
+    double dv, hv;
+    scalar_sample2(d, p, F.dO, F.dT, F.hO, F.hT, F.tf, &dv, &hv);
+    return d.buoyD * dv + d.buoyT * (hv - amb);
 }
 __global__ void k_force_mac(Dev d, Fields F, const double* amb, double dt) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -597,23 +599,20 @@ __global__ void k_adv_scalar_oct(Dev d, Fields cur, Fields nxt, double dt) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.S || ghost(d, s)) return;
     V3 o = back_trace(d, cell_pos(d, s), dt, cur);
-    nxt.dO[s] = scalar_sample(d, o, cur.dO, cur.dT, cur.tf);
-    nxt.hO[s] = scalar_sample(d, o, cur.hO, cur.hT, cur.tf);
+    scalar_sample2(d, o, cur.dO, cur.dT, cur.hO, cur.hT, cur.tf, &nxt.dO[s], &nxt.hO[s]);
 }
 __global__ void k_adv_scalar_tilt(Dev d, Fields cur, Fields nxt, const uint8_t* open, double dt) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.S || ghost(d, s) || !open[s]) return;
     V3 o = back_trace(d, vert_pos(d, s), dt, cur);
-    nxt.dT[s] = scalar_sample(d, o, cur.dO, cur.dT, cur.tf);
-    nxt.hT[s] = scalar_sample(d, o, cur.hO, cur.hT, cur.tf);
+    scalar_sample2(d, o, cur.dO, cur.dT, cur.hO, cur.hT, cur.tf, &nxt.dT[s], &nxt.hT[s]);
 }
 __global__ void k_adv_scalar_half(Dev d, Fields cur, Fields nxt, double dt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.H) return;
     int hs = d.half[i];
     V3 o = back_trace(d, vert_pos(d, hs), dt, cur);
-    nxt.dT[hs] = scalar_sample(d, o, cur.dO, cur.dT, cur.tf);
-    nxt.hT[hs] = scalar_sample(d, o, cur.hO, cur.hT, cur.tf);
+    scalar_sample2(d, o, cur.dO, cur.dT, cur.hO, cur.hT, cur.tf, &nxt.dT[hs], &nxt.hT[hs]);
 }
 // one thread per (axis, slot)
 __global__ void k_adv_mac(Dev d, Fields cur, Fields nxt, double dt) {
