@@ -14,6 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libastgrid_gpu.so")
 SOURCES = ["astg_host.cpp", "astg_step.cu", "astg_pcg.cu", "astg_extrap.cu", "astg_adjoint.cu", "astg_collider.cu",
+           "astg_layout.cu",
            "astg2d.cu", "astg2d_host.cpp"]
 HEADERS = ["astg_device.cuh", "astg_sample.cuh", "astg_launch.h", "astg2d_launch.h", "scene.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -152,180 +152,40 @@ struct astg_handle {
         int r = lres[l] - 1;
         return x >= 0 && y >= 0 && z >= 0 && x < r && y < r && z < r;
     }
-    int getUntil(int l, int x, int y, int z, bool toFinest) const {
-        int r = lres[l];
-        if (x < 0 || y < 0 || z < 0 || x >= r || y >= r || z >= r) return -1;
-        for (;;) {
-            int s = get(l, x, y, z);
-            if (s >= 0 && !(sflag[s] & SF_GHOST)) return s;
-            if (toFinest) { x <<= 1; y <<= 1; z <<= 1; l -= 1; }
-            else { x >>= 1; y >>= 1; z >>= 1; l += 1; }
-            if (l < 0 || l >= L) return -1;
-        }
-    }
 
     // ---------------------------------------------------------------- layout
-    // OctreeLayer3 (src/octree_layer3.cpp:7-88): non-ghost cells of level l are the cells whose
-    // corner finest cell has split value l, in raster order; ghosts are their 26-neighbours of
-    // level l-1 or l+1, numbered in discovery order.
+    // OctreeLayer3 (src/octree_layer3.cpp:7-88) and constrainOctreeTiltE3 (src/octree_util.cpp:38-169)
+    // are built on the device (astg_layout.cu); the host keeps copies for the set-up that follows
+    LayoutBuild lay;
     void buildLayout() {
-        lres.assign(L, 0); loff.assign(L, 0); lN.assign(L, 0); lG.assign(L, 0); ldh.assign(L, 0);
-        brick.assign(L, {});
-        int off = 0;
-        for (int l = 0; l < L; ++l) {
-            int r = res >> l;
-            lres[l] = r;
-            ldh[l] = dx * (1 << l);
-            loff[l] = off;
-            brick[l].assign((size_t)r * r * r, -1);
-            auto sp = [&](int x, int y, int z) { return split[((size_t)(z << l) * res + (y << l)) * res + (x << l)]; };
-            int n = 0;
-            for (int z = 0; z < r; ++z)
-                for (int y = 0; y < r; ++y)
-                    for (int x = 0; x < r; ++x)
-                        if (sp(x, y, z) == l) {
-                            brick[l][((size_t)z * r + y) * r + x] = off + n++;
-                            sx.push_back(x); sy.push_back(y); sz.push_back(z); slev.push_back(l); sflag.push_back(0);
-                        }
-            lN[l] = n;
-            int cIdx = n;
-            for (int i = 0; i < n; ++i) {
-                int bx = sx[off + i], by = sy[off + i], bz = sz[off + i];
-                for (int a = -1; a <= 1; ++a)
-                    for (int b = -1; b <= 1; ++b)
-                        for (int c = -1; c <= 1; ++c) {
-                            if (a == 0 && b == 0 && c == 0) continue;
-                            int nx = bx + a, ny = by + b, nz = bz + c;
-                            if (nx < 0 || ny < 0 || nz < 0 || nx >= r || ny >= r || nz >= r) continue;
-                            int& bk = brick[l][((size_t)nz * r + ny) * r + nx];
-                            if (bk >= 0) continue;
-                            int tv = sp(nx, ny, nz);
-                            if (tv == l - 1 || tv == l + 1) {
-                                bk = off + cIdx++;
-                                sx.push_back(nx); sy.push_back(ny); sz.push_back(nz); slev.push_back(l);
-                                sflag.push_back(SF_GHOST | (tv == l + 1 ? SF_FROM_COARSE : 0));
-                            }
-                        }
-            }
-            lG[l] = cIdx - n;
-            off += cIdx;
+        ldh.assign(L, 0);
+        for (int l = 0; l < L; ++l) ldh[l] = dx * (1 << l);
+        build_layout_device(split.data(), res, L, ldh.data(), allocs, lay, st);
+        S = lay.S;
+        lres.assign(lay.lres, lay.lres + L);
+        loff.assign(lay.loff, lay.loff + L);
+        lN.assign(lay.lN, lay.lN + L);
+        lG.assign(lay.lG, lay.lG + L);
+        brick = std::move(lay.hbrick);
+        sx.resize(S); sy.resize(S); sz.resize(S); slev.resize(S); sflag.resize(S);
+        for (int s = 0; s < S; ++s) {
+            const int4 q = lay.hslot[s];
+            sx[s] = q.x; sy[s] = q.y; sz[s] = q.z; slev[s] = q.w & 0xff; sflag[s] = (q.w >> 8) & 0xff;
         }
-        S = off;
-        // the fixed reduction tree folds at most 2048 chunk partials in one block
-        if (2LL * S > 2048LL * 2048LL) throw std::runtime_error("layout: too many cells for the reduction tree");
-    }
-
-    // OctreeVertexCenteredGrid3<TiltENode>::updateGhost (src/octree_vertex_centered_grid3.cpp:6-24)
-    void tiltGhostCopy(std::vector<HTilt>& t) {
-        for (int l = 0; l < L; ++l)
-            for (int i = lN[l]; i < lN[l] + lG[l]; ++i) {
-                int s = loff[l] + i;
-                int x = sx[s], y = sy[s], z = sz[s];
-                if (sflag[s] & SF_FROM_COARSE) {
-                    if ((x & 1) || (y & 1) || (z & 1)) continue;
-                    t[s] = t[req(l + 1, x >> 1, y >> 1, z >> 1)];
-                } else {
-                    t[s] = t[req(l - 1, x << 1, y << 1, z << 1)];
-                }
-            }
-    }
-
-    // constrainOctreeTiltE3 (src/octree_util.cpp:38-169)
-    void constrainTilts(std::vector<HTilt>& t, bool record) {
-        for (int s = 0; s < S; ++s) {  // T-joints at level transitions
-            if (sflag[s] & SF_GHOST) continue;
-            int l = slev[s], x = sx[s], y = sy[s], z = sz[s];
-            int minL = l, maxL = l;
-            for (int i = -1; i <= 0; ++i)
-                for (int j = -1; j <= 0; ++j)
-                    for (int k = -1; k <= 0; ++k) {
-                        int c = getUntil(l, x + i, y + j, z + k, true);
-                        if (c < 0) c = getUntil(l, x + i, y + j, z + k, false);
-                        // the packed-coordinate test "c > 0" of the reference skips level 0, (0,0,0)
-                        if (c >= 0 && !(slev[c] == 0 && sx[c] == 0 && sy[c] == 0 && sz[c] == 0)) {
-                            minL = std::min(minL, slev[c]);
-                            maxL = std::max(maxL, slev[c]);
-                        }
-                    }
-            if (minL < l || (maxL > l && !(x & 1) && !(y & 1) && !(z & 1))) {
-                HTilt n = t[s];
-                n.put(TF_TJOINT, true);
-                n.e = ldh[minL];
-                n.put(TF_FIXED, true);
-                n.put(TF_CLOSED, false);
-                t[s] = n;
-                if (record) tj.push_back(s);
-            }
+        lay.hslot.clear();
+        lay.hslot.shrink_to_fit();
+        // both buffers of the tilt-E grid are constrained alike (src/octree_omnigrid_solver3.cpp:92-94)
+        te[0].resize(S);
+        for (int s = 0; s < S; ++s) {
+            te[0][s].e = lay.te[s];
+            te[0][s].f = lay.tf[s];
+            te[0][s].dir = lay.tdir[s];
         }
-        for (int s = 0; s < S; ++s) {  // tilts closed by T-joints
-            if ((sflag[s] & SF_GHOST) || !t[s].has(TF_TJOINT)) continue;
-            int l = slev[s], x = sx[s], y = sy[s], z = sz[s];
-            if (t[s].e < ldh[l]) { l -= 1; x *= 2; y *= 2; z *= 2; }
-            for (int i = 0; i < 6; ++i) {
-                int q = get(l, x + OCT_NB_H[i][0], y + OCT_NB_H[i][1], z + OCT_NB_H[i][2]);
-                if (q < 0) continue;
-                HTilt n = t[q];
-                n.setE(0);
-                n.put(TF_FIXED, true);
-                n.put(TF_CLOSED_BY_T, true);
-                t[q] = n;
-            }
-        }
-        tiltGhostCopy(t);
-        for (int s = 0; s < S; ++s) {  // half tilts on coarse faces surrounded by T-joints
-            if ((sflag[s] & SF_GHOST) || !t[s].has(TF_TJOINT)) continue;
-            int l = slev[s];
-            bool coarse = t[s].e < ldh[l];
-            int ci[3] = {coarse ? sx[s] : sx[s] >> 1, coarse ? sy[s] : sy[s] >> 1, coarse ? sz[s] : sz[s] >> 1};
-            int lc = l + (!coarse);
-            for (int axis = 0; axis < 3; ++axis) {
-                if (ci[axis] == 0 || ci[axis] == lres[l - coarse] - 1) continue;
-                bool flag = true;
-                for (int i = 0; i <= 1 && flag; ++i)
-                    for (int j = 0; j <= 1 && flag; ++j) {
-                        if (i == 0 && j == 0) continue;
-                        int id[3] = {ci[0], ci[1], ci[2]};
-                        id[(axis + 1) % 3] += i;
-                        id[(axis + 2) % 3] += j;
-                        int c = lc < L ? getUntil(lc, id[0], id[1], id[2], true) : -1;
-                        if (c < 0 && lc < L) c = getUntil(lc, id[0], id[1], id[2], false);
-                        if (c < 0 || !t[c].has(TF_TJOINT)) flag = false;
-                    }
-                if (flag) {
-                    int nb[3] = {ci[0], ci[1], ci[2]};
-                    nb[axis] -= 1;
-                    int c = lc < L ? getUntil(lc, ci[0], ci[1], ci[2], true) : -1;
-                    int c1 = lc < L ? getUntil(lc, nb[0], nb[1], nb[2], true) : -1;
-                    int lvc = c >= 0 ? slev[c] : 15;  // UNPACK_LEVEL3(-1)
-                    if (c1 < 0 || lvc == slev[c1]) flag = false;
-                }
-                if (!flag) continue;
-                int id[3] = {ci[0] * 2, ci[1] * 2, ci[2] * 2};
-                id[(axis + 1) % 3] += 1;
-                id[(axis + 2) % 3] += 1;
-                int hl = l - coarse;
-                int hs = get(hl, id[0], id[1], id[2]);
-                if (hs < 0) continue;
-                HTilt n = t[hs];
-                n.put(TF_CLOSED, true);
-                n.put(TF_HALF, true);
-                n.put(TF_FIXED, true);
-                n.dir = axis + (coarse ? 3 : 0);
-                n.e = ldh[hl];
-                t[hs] = n;
-                if (record) half.push_back(hs);
-                int tp[3] = {id[0], id[1], id[2]};
-                tp[axis] += n.dir < 3 ? 1 : -1;
-                int ts = req(hl, tp[0], tp[1], tp[2]);
-                if (record && std::find(cbh.begin(), cbh.end(), ts) == cbh.end()) cbh.push_back(ts);
-                HTilt m = t[ts];
-                m.setE(0);
-                m.put(TF_CLOSED_BY_T, true);
-                m.dir = -1;
-                m.put(TF_FIXED, true);
-                t[ts] = m;
-            }
-        }
+        te[1] = te[0];
+        half = lay.half;
+        tj = lay.tj;
+        cbh = lay.cbh;
+        lay.te.clear(); lay.tf.clear(); lay.tdir.clear();
     }
 
     // Constants::init least-squares tables (src/constants.cpp:170-256), inverted through a
@@ -412,13 +272,8 @@ struct astg_handle {
 
         buildLayout();
         buildTables();
-        for (int b = 0; b < 2; ++b) te[b].assign(S, HTilt());
         tOpen.assign(S, 0);
         tFixed.assign(S, 0);
-        constrainTilts(te[0], true);
-        tiltGhostCopy(te[0]);
-        constrainTilts(te[1], false);
-        tiltGhostCopy(te[1]);
         H = (int)half.size();
         {
             std::vector<int> hs = half;
@@ -470,18 +325,6 @@ struct astg_handle {
     }
 
     void uploadAll() {
-        // finest non-ghost level containing each finest cell (OctreeGridLayout3::levelCoordinate)
-        std::vector<uint8_t> locate((size_t)res * res * res, 0xff);
-        for (int z = 0; z < res; ++z)
-            for (int y = 0; y < res; ++y)
-                for (int x = 0; x < res; ++x) {
-                    for (int l = 0; l < L; ++l) {
-                        int s = get(l, x >> l, y >> l, z >> l);
-                        if (s >= 0 && !(sflag[s] & SF_GHOST)) { locate[((size_t)z * res + y) * res + x] = (uint8_t)l; break; }
-                    }
-                }
-        std::vector<int4> slot(S);
-        for (int s = 0; s < S; ++s) slot[s] = make_int4(sx[s], sy[s], sz[s], slev[s] | (sflag[s] << 8));
         std::vector<uint8_t> halfMark(S, 0);
         for (int hs : half) halfMark[hs] = 1;
         // half tilts facing each coarse octagon, in list order (assembly, :572-581)
@@ -516,7 +359,7 @@ struct astg_handle {
         d.dx = dx;
         for (int l = 0; l < L; ++l) {
             d.lres[l] = lres[l]; d.loff[l] = loff[l]; d.lN[l] = lN[l]; d.lG[l] = lG[l]; d.ldh[l] = ldh[l];
-            d.brick[l] = upload(brick[l]);
+            d.brick[l] = lay.brick[l];  // built on the device
         }
         // power-of-two spacings: their reciprocals are exact, so x * (1 / h) == x / h (over_h)
         auto pow2 = [](double v) { int e; return std::frexp(v, &e) == 0.5; };
@@ -524,8 +367,8 @@ struct astg_handle {
         for (int l = 0; l < L; ++l) d.pow2 = d.pow2 && pow2(ldh[l]);
         d.dxInv = 1.0 / dx;
         for (int l = 0; l < L; ++l) d.ldhInv[l] = 1.0 / ldh[l];
-        d.locate = upload(locate);
-        d.slot = upload(slot);
+        d.locate = lay.locate;
+        d.slot = lay.slot;
         d.half = upload(half);
         d.halfMark = upload(halfMark);
         d.tj = upload(tj);

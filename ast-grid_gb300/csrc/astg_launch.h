@@ -202,6 +202,27 @@ void launch_mean_temperature_ref(const Dev& d, const double* hO, int workers, do
 void launch_max_face(const Dev& d, const double* mac, unsigned long long* out, cudaStream_t st);
 // collider (astg_collider.cu): per-slot bits and cut-cell weights once per collider; the per-step
 // wipe and inside-solid constraints (before: 3 * S doubles of scratch for the MAC projection)
+// OctreeLayer3 and constrainOctreeTiltE3 built on the device (astg_layout.cu).  Device arrays named
+// here are allocated into the caller's list (freed with it); the host copies feed the host-side
+// set-up that follows (tables, weights, initial velocity).
+struct LayoutBuild {
+    int L = 0, res = 0, S = 0;
+    int lres[MAXL] = {}, loff[MAXL] = {}, lN[MAXL] = {}, lG[MAXL] = {};
+    int* brick[MAXL] = {};   // device, per level res_l^3 slots or -1
+    int4* slot = nullptr;    // device, S
+    uint8_t* locate = nullptr;  // device, res^3: finest non-ghost level of each finest cell
+    std::vector<int4> hslot;
+    std::vector<std::vector<int>> hbrick;
+    std::vector<double> te;  // tilt-E size, flags and half direction after the constraint
+    std::vector<uint32_t> tf;
+    std::vector<int> tdir;
+    std::vector<int> half, tj, cbh;
+};
+void build_layout_device(const int32_t* split, int res, int L, const double* ldh, std::vector<void*>& keep,
+                         LayoutBuild& out, cudaStream_t st);
+// out = exclusive scan of in[0..n), *total = the sum; bsum holds ceil(n / 1024) ints
+void exclusive_scan(const int* in, int* out, int* bsum, int* total, long long n, cudaStream_t st);
+
 // the SDF grid of a sphere collider at the finest cell centres (res^3 doubles)
 void launch_collider_sphere_sdf(int res, double cx, double cy, double cz, double r, double* sdf, cudaStream_t st);
 void launch_collider_setup(const Dev& d, const int* halfDir, uint16_t* mask, double* wMac, double* wTilt,

@@ -514,7 +514,7 @@ __global__ void k_scan_add(int* out, const int* bsum, long long n) {
     if (i < n) out[i] += bsum[blockIdx.x];
 }
 // out = exclusive scan of in[0..n); *total = sum.  bsum needs ceil(n/1024) ints.
-static void exclusive_scan(const int* in, int* out, int* bsum, int* total, long long n, cudaStream_t st) {
+void exclusive_scan(const int* in, int* out, int* bsum, int* total, long long n, cudaStream_t st) {
     int nb = (int)((n + SCAN_B - 1) / SCAN_B);
     ASTG_LAUNCH(k_scan_block<<<nb, SCAN_B, 0, st>>>(in, out, bsum, n));
     ASTG_LAUNCH(k_scan_sums<<<1, SCAN_B, 0, st>>>(bsum, nb, total));
