@@ -6,11 +6,12 @@
 // 0.0, the lanes are folded by halving strides (t += t + s for s = 128 ... 1) and the chunk partials
 // are reduced by the same rule.  The CPU oracle implements the same tree, so the FP64 solve is
 // reproducible bit for bit.  Matrix rows are summed sequentially in column order, and the
-// triangular sweeps and the factorisation apply their updates in the reference's order.  In the
-// sweeps each update z_i -= L_ij z_j is one fused multiply-subtract (fma(-L_ij, z_j, z_i), one
-// rounding instead of two; the oracle's library-order mode does the same): FP64 issue is the
-// scarce resource of the sweeps on this part, and the fused form halves it (measured 0.58 ->
-// 0.46 ms per application at the 256^3-equivalent size).
+// triangular sweeps and the factorisation apply their updates in the reference's order.  Every
+// product the PCG accumulates is one fused multiply-add (one rounding instead of two; the
+// oracle's library-order mode does the same): each sweep update z_i -= L_ij z_j as
+// fma(-L_ij, z_j, z_i), each CSR row term, each dot-product lane term and the vector updates.
+// FP64 issue is the scarce resource on this part, and the fused form halves it (sweeps: measured
+// 0.58 -> 0.46 ms per application at the 256^3-equivalent size).
 //
 // Reference order (astg_set_reduction_order, P.refOrder): the same solve in the reference's own
 // arithmetic, for bit-for-bit parity with it: the dot products in Eigen 3.3.7's order (two SSE2
@@ -204,7 +205,7 @@ __global__ void k_tree_sum(const double* a, const long long* nptr, long long nco
     double r = block_tree(acc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = r;
 }
-// sum of a[i] * b[i]
+// sum of a[i] * b[i]; each lane accumulates with fused multiply-adds (the library's order)
 __global__ void k_tree_dot(const double* a, const double* b, const int* nptr, double* part) {
     __shared__ double sh[RED_LANES];
     long long n = *nptr;
@@ -213,7 +214,7 @@ __global__ void k_tree_dot(const double* a, const double* b, const int* nptr, do
     double acc = 0.0;
     for (int k = 0; k < RED_PER_LANE; ++k) {
         long long i = base + threadIdx.x + (long long)RED_LANES * k;
-        if (i < n) acc = acc + a[i] * b[i];
+        if (i < n) acc = fma(a[i], b[i], acc);
     }
     double r = block_tree(acc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = r;
@@ -1817,6 +1818,15 @@ __device__ __forceinline__ double chunk_fold(double acc, double* sh) {
     }
     return sh[0];
 }
+// FUSED (the library's order): each product-accumulate is one fused multiply-add; otherwise (the
+// reference's order) a product, then an addition, as its CSR multiply computes them
+template <bool FUSED>
+__device__ __forceinline__ double mac_add(double acc, double a, double b) {
+    if (FUSED) return fma(a, b, acc);
+    double prod = a * b;
+    return acc + prod;
+}
+template <bool FUSED>
 __global__ void __launch_bounds__(SPMV_THREADS) k_spmv_dot(Proj P, const double* s, double* z, double* part) {
     __shared__ double ys[RED_CHUNK];
     __shared__ double sh[RED_LANES];
@@ -1828,7 +1838,7 @@ __global__ void __launch_bounds__(SPMV_THREADS) k_spmv_dot(Proj P, const double*
         long long i = base + k;
         double t = 0;
         if (i < n) {
-            for (int q = P.rowPtr[i]; q < P.rowPtr[i + 1]; ++q) t += P.val[q] * s[P.col[q]];
+            for (int q = P.rowPtr[i]; q < P.rowPtr[i + 1]; ++q) t = mac_add<FUSED>(t, P.val[q], s[P.col[q]]);
             z[i] = t;
         }
         ys[k] = t;
@@ -1839,7 +1849,7 @@ __global__ void __launch_bounds__(SPMV_THREADS) k_spmv_dot(Proj P, const double*
     if (tl < RED_LANES)
         for (int k = 0; k < RED_PER_LANE; ++k) {
             long long i = base + tl + (long long)RED_LANES * k;
-            if (i < n) acc = acc + s[i] * ys[tl + RED_LANES * k];
+            if (i < n) acc = mac_add<FUSED>(acc, s[i], ys[tl + RED_LANES * k]);
         }
     double r = chunk_fold(acc, sh);
     if (tl == 0) part[blockIdx.x] = r;
@@ -1852,6 +1862,7 @@ __global__ void k_alpha(Proj P, const double* part) {
     double dsz = fold_partials(part, m, sh);
     if (threadIdx.x == 0) P.sc[SC_ALPHA] = P.sc[SC_RHO] / dsz;
 }
+template <bool FUSED>
 __global__ void k_update_xr(Proj P, double* x, double* r, const double* s, const double* z) {
     if (*P.done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1859,8 +1870,8 @@ __global__ void k_update_xr(Proj P, double* x, double* r, const double* s, const
     double alpha = P.sc[SC_ALPHA];
     double v = 0;
     if (i < n) {
-        x[i] += alpha * s[i];
-        double ri = r[i] + -alpha * z[i];
+        x[i] = mac_add<FUSED>(x[i], alpha, s[i]);
+        double ri = mac_add<FUSED>(r[i], -alpha, z[i]);
         r[i] = ri;
         if (P.pcActive) P.rl[P.pos[i]] = ri;
         if (P.wave) wave_put_r(P, i, ri);
@@ -1901,11 +1912,12 @@ __global__ void k_beta(Proj P, const double* part) {
         P.sc[SC_RHO] = rn;
     }
 }
+template <bool FUSED>
 __global__ void k_update_s(Proj P, double* s, const double* z) {
     if (*P.done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *P.nDof) return;
-    s[i] = z[i] + P.sc[SC_BETA] * s[i];
+    s[i] = mac_add<FUSED>(z[i], P.sc[SC_BETA], s[i]);
 }
 __global__ void k_reset_counter(int* c) { *c = 0; }
 
@@ -2127,17 +2139,20 @@ int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& e
     auto body = [&](int nb, KProf* pf) {
         for (int it = 0; it < nb; ++it) {
             prof_begin(pf, 2, st);
-            ASTG_LAUNCH(k_spmv_dot<<<chunks, SPMV_THREADS, 0, st>>>(P, s, z, P.part));
+            if (P.refOrder) ASTG_LAUNCH(k_spmv_dot<false><<<chunks, SPMV_THREADS, 0, st>>>(P, s, z, P.part));
+            else ASTG_LAUNCH(k_spmv_dot<true><<<chunks, SPMV_THREADS, 0, st>>>(P, s, z, P.part));
             prof_end(pf, st);
             if (P.refOrder) launch_dot_ref(s, z, P.nDof, P.part, st);
             ASTG_LAUNCH(k_alpha<<<1, RED_LANES, 0, st>>>(P, P.part));
-            ASTG_LAUNCH(k_update_xr<<<nblk(maxRows), TB, 0, st>>>(P, x, r, s, z));
+            if (P.refOrder) ASTG_LAUNCH(k_update_xr<false><<<nblk(maxRows), TB, 0, st>>>(P, x, r, s, z));
+            else ASTG_LAUNCH(k_update_xr<true><<<nblk(maxRows), TB, 0, st>>>(P, x, r, s, z));
             ASTG_LAUNCH(k_check<<<1, 1, 0, st>>>(P, maxIter));
             precond(d, P, r, z, epoch, st, pf);
             if (P.refOrder) launch_dot_ref(z, r, P.nDof, P.part, st);
             else ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
             ASTG_LAUNCH(k_beta<<<1, RED_LANES, 0, st>>>(P, P.part));
-            ASTG_LAUNCH(k_update_s<<<nblk(maxRows), TB, 0, st>>>(P, s, z));
+            if (P.refOrder) ASTG_LAUNCH(k_update_s<false><<<nblk(maxRows), TB, 0, st>>>(P, s, z));
+            else ASTG_LAUNCH(k_update_s<true><<<nblk(maxRows), TB, 0, st>>>(P, s, z));
         }
     };
     BatchGraph graph;

@@ -12,7 +12,8 @@
 // Two reduction modes, as in oracle/smoke_oracle.cpp: 0 = the reference's own order (the PCG's
 // dot products summed in the per-worker slices of ThreadPool::parallelForTFWithCoreID, then the
 // slice sums in order, include/pcgsolver/blas_wrapper.h:17-38 with USE_TASKFLOW), 1 = the CUDA
-// library's (its fixed reduction tree, one fused multiply-subtract per MIC(0) sweep update).
+// library's (its fixed reduction tree, and one fused multiply-add for every product it accumulates:
+// MIC(0) sweep updates, CSR rows, dot-product lanes and the PCG's vector updates).
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -60,7 +61,7 @@ static void bary(double x, int high, int* i, double* f) {
 // fixed reduction tree of the CUDA library
 static const int RED_LANES = 256, RED_PER_LANE = 8, RED_CHUNK = RED_LANES * RED_PER_LANE;
 template <class F>
-static double treeReduce(size_t n, const F& elem) {
+static double treeReduce(size_t n, const F& step) {
     size_t chunks = (n + RED_CHUNK - 1) / RED_CHUNK;
     std::vector<double> part(chunks);
     std::vector<double> lane(RED_LANES);
@@ -74,7 +75,7 @@ static double treeReduce(size_t n, const F& elem) {
             double acc = 0.0;
             for (int k = 0; k < RED_PER_LANE; ++k) {
                 size_t i = c * RED_CHUNK + t + (size_t)RED_LANES * k;
-                if (i < n) acc = acc + elem(i);
+                if (i < n) acc = step(acc, i);
             }
             lane[t] = acc;
         }
@@ -219,9 +220,16 @@ struct Pcg {
             z[i] *= F.invdiag[i];
         }
     }
+    // acc + a * b: one fused multiply-add in the library's order, a product then an addition in the
+    // reference's (r -= alpha z is r + (-alpha) z there, the same number)
+    double fmadd(double acc, double a, double b) const {
+        if (reduceMode != 0) return std::fma(a, b, acc);
+        double prod = a * b;
+        return acc + prod;
+    }
     double dot(const std::vector<double>& a, const std::vector<double>& b) const {
         if (reduceMode == 0) return workerDot(a, b, workers);
-        return treeReduce(a.size(), [&](size_t i) { return a[i] * b[i]; });
+        return treeReduce(a.size(), [&](double acc, size_t i) { return std::fma(a[i], b[i], acc); });
     }
     static double absmax(const std::vector<double>& a) {
         double m = 0;
@@ -245,20 +253,20 @@ struct Pcg {
         for (it = 0; it < maxIter; ++it) {
             for (int i = 0; i < n; ++i) {
                 double t = 0;
-                for (size_t j = 0; j < A.idx[i].size(); ++j) t += A.val[i][j] * s[A.idx[i][j]];
+                for (size_t j = 0; j < A.idx[i].size(); ++j) t = fmadd(t, A.val[i][j], s[A.idx[i][j]]);
                 z[i] = t;
             }
             double alpha = rho / dot(s, z);
             for (int i = 0; i < n; ++i) {
-                x[i] += alpha * s[i];
-                r[i] -= alpha * z[i];
+                x[i] = fmadd(x[i], alpha, s[i]);
+                r[i] = fmadd(r[i], -alpha, z[i]);
             }
             resid = absmax(r);
             if (resid <= tol) { iters = it + 1; return; }
             precond(r, z);
             double rn = dot(z, r);
             double beta = rn / rho;
-            for (int i = 0; i < n; ++i) z[i] += beta * s[i];
+            for (int i = 0; i < n; ++i) z[i] = fmadd(z[i], beta, s[i]);
             s.swap(z);
             rho = rn;
         }

@@ -94,7 +94,8 @@ class Oracle:
                  reduce_mode=0, ref_workers=8, openmp=False):
         """reduce_mode 0 follows the reference's own arithmetic order (Eigen's dot, per-worker
         partial sums over ref_workers workers); 1 follows the CUDA library's (its fixed reduction
-        tree, and one fused multiply-subtract per update of the MIC(0) sweeps)."""
+        tree, and one fused multiply-add for every product the PCG accumulates: MIC(0) sweep
+        updates, CSR rows, dot-product lanes, vector updates)."""
         p = _Params(tol, buoy_d, buoy_t, decay, rho, noise, source[0], source[1], source[2], source[3], seed,
                     max_iter, 1 if tilt_adaptivity else 0, closed_mask, reduce_mode, ref_workers)
         self._lib = lib(openmp)

@@ -150,7 +150,8 @@ struct Params {
     //      include/thread_pool.h:319-348) with refWorkers workers;
     //  1 = the fixed reduction tree of the CUDA library (chunks of 2048, 256 lanes x 8
     //      strided elements, binary tree over the lanes, chunk partials reduced the same way),
-    //      and the library's MIC(0) sweeps: each update one fused multiply-subtract.
+    //      and one fused multiply-add for every product the PCG accumulates: each MIC(0) sweep
+    //      update, each CSR row term, each dot-product lane term and the vector updates.
     int reduceMode = 0;
     int refWorkers = 8;
 };
@@ -187,12 +188,13 @@ static double eigenDot(const double* a, const double* b, size_t n) {
 }
 
 // The CUDA library's fixed reduction tree.  Element i belongs to chunk i / 2048 and lane
-// (i % 2048) % 256; a lane adds its (up to) eight elements in index order starting from 0,
-// the 256 lanes are folded by halving strides (lane t += lane t + s for s = 128 ... 1), and the
-// chunk partials are reduced by the same rule until one value is left.
+// (i % 2048) % 256; a lane accumulates its (up to) eight elements in index order starting from 0
+// with step(acc, i) (a sum adds the element; a dot is one fused multiply-add per element), the 256
+// lanes are folded by halving strides (lane t += lane t + s for s = 128 ... 1), and the chunk
+// partials are added by the same rule until one value is left.
 static const int RED_LANES = 256, RED_PER_LANE = 8, RED_CHUNK = RED_LANES * RED_PER_LANE;
 template <class F>
-static double treeReduce(size_t n, const F& elem) {
+static double treeReduce(size_t n, const F& step) {
     if (n == 0) return 0.0;
     std::vector<double> part((n + RED_CHUNK - 1) / RED_CHUNK);
     double lane[RED_LANES];
@@ -202,7 +204,7 @@ static double treeReduce(size_t n, const F& elem) {
             double acc = 0.0;
             for (int k = 0; k < RED_PER_LANE; ++k) {
                 size_t i = base + t + (size_t)RED_LANES * k;
-                if (i < n) acc = acc + elem(i);
+                if (i < n) acc = step(acc, i);
             }
             lane[t] = acc;
         }
@@ -1411,7 +1413,7 @@ public:
         for (int l = 0; l < L; ++l) {
             const double* h = &hO[c][loff[l]];
             size_t nl = lN[l] + lG[l];
-            double sum = P.reduceMode == 0 ? refSum(h, nl, P.refWorkers) : treeReduce(nl, [&](size_t i) { return h[i]; });
+            double sum = P.reduceMode == 0 ? refSum(h, nl, P.refWorkers) : treeReduce(nl, [&](double acc, size_t i) { return acc + h[i]; });
             amb += sum * (l == 0 ? 1 : 8);
             count += (long long)(lN[l] + lG[l]) * (l == 0 ? 1 : 8);
         }
@@ -1767,9 +1769,16 @@ public:
             z[i] *= F.invdiag[i];
         }
     }
+    // acc + a * b: in the library's order one fused multiply-add (CSR rows, dots, vector updates), in
+    // the reference's a product, then an addition
+    double fmadd(double acc, double a, double b) const {
+        if (P.reduceMode != 0) return std::fma(a, b, acc);
+        double prod = a * b;
+        return acc + prod;
+    }
     double dotv(const std::vector<double>& a, const std::vector<double>& b) const {
         if (P.reduceMode == 0) return eigenDot(a.data(), b.data(), a.size());
-        return treeReduce(a.size(), [&](size_t i) { return a[i] * b[i]; });
+        return treeReduce(a.size(), [&](double acc, size_t i) { return std::fma(a[i], b[i], acc); });
     }
     static double absmax(const std::vector<double>& a) {
         double m = 0;
@@ -1806,17 +1815,17 @@ public:
     #pragma omp parallel for schedule(dynamic, 256)
             for (int i = 0; i < n; ++i) {
                 double t = 0;
-                for (int j = csrPtr[i]; j < csrPtr[i + 1]; ++j) t += csrVal[j] * s[csrCol[j]];
+                for (int j = csrPtr[i]; j < csrPtr[i + 1]; ++j) t = fmadd(t, csrVal[j], s[csrCol[j]]);
                 z[i] = t;
             }
             double alpha = rho / dotv(s, z);
-            for (int i = 0; i < n; ++i) { p[i] += alpha * s[i]; r[i] += -alpha * z[i]; }
+            for (int i = 0; i < n; ++i) { p[i] = fmadd(p[i], alpha, s[i]); r[i] = fmadd(r[i], -alpha, z[i]); }
             resid = absmax(r);
             if (resid <= tol) { pcgIters = it + 1; pcgErr = resid; pcgOk = true; return; }
             applyPrecond(r, z);
             double rn = dotv(z, r);
             double beta = rn / rho;
-            for (int i = 0; i < n; ++i) z[i] += beta * s[i];
+            for (int i = 0; i < n; ++i) z[i] = fmadd(z[i], beta, s[i]);
             s.swap(z);
             rho = rn;
         }
