@@ -1775,15 +1775,28 @@ __global__ void k_zero_vec(double* a, const int* nptr) {
     if (i < *nptr) a[i] = 0;
 }
 // max |a| over [0, n): non-negative doubles order like their bit patterns
-__global__ void k_absmax(const double* a, const int* nptr, unsigned long long* out) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double v = 0;
-    if (i < *nptr) v = fabs(a[i]);
+// the largest of the block's v (all threads of the block call it) into *out: a warp maximum by
+// shuffles, the block's over its warps in shared memory, one atomic per block (non-negative doubles
+// order as their bit patterns).  One atomic per warp on the same word serialised at the L2.
+__device__ __forceinline__ void block_absmax_to(double v, unsigned long long* out) {
+    __shared__ double wm[32];
     for (int o = 16; o > 0; o >>= 1) {
         double w = __shfl_xor_sync(0xffffffffu, v, o);
         v = w > v ? w : v;
     }
-    if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(out, (unsigned long long)__double_as_longlong(v));
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = wm[0];
+        for (int k = 1; k < (int)((blockDim.x + 31) >> 5); ++k) m = wm[k] > m ? wm[k] : m;
+        if (m > 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+    }
+}
+__global__ void k_absmax(const double* a, const int* nptr, unsigned long long* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0;
+    if (i < *nptr) v = fabs(a[i]);
+    block_absmax_to(v, out);
 }
 __global__ void k_pcg_start(Proj P, const double* partRho, double tolFactor) {
     __shared__ double sh[RED_LANES];
@@ -1877,11 +1890,7 @@ __global__ void k_update_xr(Proj P, double* x, double* r, const double* s, const
         if (P.wave) wave_put_r(P, i, ri);
         v = fabs(ri);
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        double w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = w > v ? w : v;
-    }
-    if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(P.amax, (unsigned long long)__double_as_longlong(v));
+    block_absmax_to(v, P.amax);
 }
 __global__ void k_check(Proj P, int maxIter) {
     if (*P.done) return;
@@ -2180,7 +2189,9 @@ namespace astg {
 // (FP32 matrix, FP32 MIC(0) factor rounded from the FP64 one, FP32 vectors; dot products reduced
 // in FP64 by the fixed tree; alpha and beta in FP64) until its residual drops below
 // max(1e-5 |r|_inf, 0.5 tol |b|_inf), then x += e and r = b - A x in FP64.  The stopping test is
-// the reference's, on the FP64 residual.
+// the reference's, on the FP64 residual.  The inner solve owes no bit pattern to anything, so its
+// FP32 row sums and vector updates and the FP64 lanes of its dots are fused multiply-adds
+// (fmaf / fma written out: the library is compiled without contraction for the FP64 paths).
 constexpr double MIXED_INNER_REDUCTION = 1e-5;
 constexpr int MIXED_MAX_OUTER = 20;
 __global__ void k_to_f32(const double* a, float* b, const int* nptr) {
@@ -2198,11 +2209,7 @@ __global__ void k_resid64(Proj P, const double* x, double* r) {
         r[i] = ri;
         v = fabs(ri);
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        double w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = w > v ? w : v;
-    }
-    if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(P.amax, (unsigned long long)__double_as_longlong(v));
+    block_absmax_to(v, P.amax);
 }
 // start of an inner solve: r32 = r (also in walk order), e32 = 0
 __global__ void k_inner_init(Proj P, const double* r) {
@@ -2222,7 +2229,7 @@ __global__ void k_tree_dot32(const float* a, const float* b, const int* nptr, do
     double acc = 0.0;
     for (int k = 0; k < RED_PER_LANE; ++k) {
         long long i = base + threadIdx.x + (long long)RED_LANES * k;
-        if (i < n) acc = acc + (double)a[i] * (double)b[i];
+        if (i < n) acc = fma((double)a[i], (double)b[i], acc);
     }
     double r = block_tree(acc, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = r;
@@ -2256,7 +2263,7 @@ __global__ void __launch_bounds__(SPMV_THREADS) k_spmv32_dot(Proj P, const float
         long long i = base + k;
         float t = 0;
         if (i < n) {
-            for (int c = P.rowPtr[i]; c < P.rowPtr[i + 1]; ++c) t += P.val32[c] * s[P.col[c]];
+            for (int c = P.rowPtr[i]; c < P.rowPtr[i + 1]; ++c) t = fmaf(P.val32[c], s[P.col[c]], t);
             q[i] = t;
         }
         ys[k] = t;
@@ -2267,7 +2274,7 @@ __global__ void __launch_bounds__(SPMV_THREADS) k_spmv32_dot(Proj P, const float
     if (tl < RED_LANES)
         for (int k = 0; k < RED_PER_LANE; ++k) {
             long long i = base + tl + (long long)RED_LANES * k;
-            if (i < n) acc = acc + (double)s[i] * (double)ys[tl + RED_LANES * k];
+            if (i < n) acc = fma((double)s[i], (double)ys[tl + RED_LANES * k], acc);
         }
     double r = chunk_fold(acc, sh);
     if (tl == 0) part[blockIdx.x] = r;
@@ -2278,22 +2285,18 @@ __global__ void k_update_er32(Proj P) {
     float alpha = (float)P.sc[SC_ALPHA];
     double v = 0;
     if (i < *P.nDof) {
-        P.e32[i] += alpha * P.s32[i];
-        float ri = P.r32[i] - alpha * P.q32[i];
+        P.e32[i] = fmaf(alpha, P.s32[i], P.e32[i]);
+        float ri = fmaf(-alpha, P.q32[i], P.r32[i]);
         P.r32[i] = ri;
         P.rl32[P.pos[i]] = ri;
         v = fabs((double)ri);
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        double w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = w > v ? w : v;
-    }
-    if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(P.amax, (unsigned long long)__double_as_longlong(v));
+    block_absmax_to(v, P.amax);
 }
 __global__ void k_update_s32(Proj P) {
     if (*P.done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < *P.nDof) P.s32[i] = P.z32[i] + (float)P.sc[SC_BETA] * P.s32[i];
+    if (i < *P.nDof) P.s32[i] = fmaf((float)P.sc[SC_BETA], P.s32[i], P.z32[i]);
 }
 __global__ void k_add_correction(Proj P, double* x) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
