@@ -2040,6 +2040,7 @@ __global__ void k_plan_fill(Proj P) {
     }
 }
 constexpr int PLAN_MAXU = 16;  // upper entries of a column applied from registers (more: in place)
+constexpr int FACTOR_ROW = 24;  // a row's upper entries updated in a thread-local copy (longer rows: in place)
 __global__ void k_mic_factor_plan(Dev d, Proj P, double omega, double minDiag, int epoch) {
     int n = *P.nDof;
     for (;;) {
@@ -2050,6 +2051,14 @@ __global__ void k_mic_factor_plan(Dev d, Proj P, double omega, double minDiag, i
         int upj = dgj >= 0 ? dgj + 1 : rj1;
         double invd = P.invdiag[j];
         int lev = 0;
+        // row j's upper entries are written by this thread alone until its flag is set: they are
+        // updated in a thread-local copy (L1) instead of read-modify-writes through L2, the same
+        // operations in the same order
+        const int nup = rj1 - upj;
+        const bool own = nup <= FACTOR_ROW;
+        double up[FACTOR_ROW];
+        if (own)
+            for (int q = 0; q < nup; ++q) up[q] = P.Lv[upj + q];
         for (int qq = rj0; qq < rj1; ++qq) {
             int k = P.col[qq];
             if (k >= j) break;
@@ -2074,14 +2083,20 @@ __global__ void k_mic_factor_plan(Dev d, Proj P, double omega, double minDiag, i
                 int c = code[u] & 3;
                 if (c == PLAN_MISSING) missing += lv[u];
                 else if (c == PLAN_DIAG) invd -= mult * lv[u];
-                else if (c == PLAN_MATCH) P.Lv[upj + (code[u] >> 2)] -= mult * lv[u];
+                else if (c == PLAN_MATCH) {
+                    if (own) up[code[u] >> 2] -= mult * lv[u];
+                    else P.Lv[upj + (code[u] >> 2)] -= mult * lv[u];
+                }
             }
             for (int u = PLAN_MAXU; u < m; ++u) {
                 int cu = P.plan[pp + u], c = cu & 3;
                 double v = P.Lv[a0 + u];
                 if (c == PLAN_MISSING) missing += v;
                 else if (c == PLAN_DIAG) invd -= mult * v;
-                else if (c == PLAN_MATCH) P.Lv[upj + (cu >> 2)] -= mult * v;
+                else if (c == PLAN_MATCH) {
+                    if (own) up[cu >> 2] -= mult * v;
+                    else P.Lv[upj + (cu >> 2)] -= mult * v;
+                }
             }
             invd -= omega * mult * missing;
         }
@@ -2089,8 +2104,13 @@ __global__ void k_mic_factor_plan(Dev d, Proj P, double omega, double minDiag, i
         if (ad != 0) {
             if (invd < minDiag * ad) invd = 1 / sqrt(ad);
             else invd = 1 / sqrt(invd);
-            for (int q = upj; q < rj1; ++q) P.Lv[q] *= invd;
+            if (own)
+                for (int q = 0; q < nup; ++q) up[q] *= invd;
+            else
+                for (int q = upj; q < rj1; ++q) P.Lv[q] *= invd;
         }
+        if (own)
+            for (int q = 0; q < nup; ++q) P.Lv[upj + q] = up[q];
         P.invdiag[j] = invd;
         P.level[j] = lev;
         __threadfence();
