@@ -178,6 +178,27 @@ __device__ __forceinline__ T sweep_update(bool unfused, T acc, T v, T zk) {
     return fma(-v, zk, acc);
 }  // ~seconds at nanosleep(64): far above any real wait
 
+// ------------------------------------------------------------------ programmatic dependent launch
+// The PCG's per-iteration kernels are launched so that each may be scheduled while its predecessor
+// on the stream finishes (its implicit trigger is the predecessor's completion); the kernel's first
+// statement waits for that predecessor's results to be visible.  Launched without the attribute
+// (or outside a dependent pair) the wait returns at once.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*k)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    ++g_launches;
+    cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 // ------------------------------------------------------------------ fixed-tree reduction
 __device__ inline double block_tree(double v, double* sh) {
     int t = threadIdx.x;
@@ -207,6 +228,7 @@ __global__ void k_tree_sum(const double* a, const long long* nptr, long long nco
 }
 // sum of a[i] * b[i]; each lane accumulates with fused multiply-adds (the library's order)
 __global__ void k_tree_dot(const double* a, const double* b, const int* nptr, double* part) {
+    grid_dep_wait();
     __shared__ double sh[RED_LANES];
     long long n = *nptr;
     long long base = (long long)blockIdx.x * RED_CHUNK;
@@ -1387,6 +1409,7 @@ __device__ __forceinline__ void pca_solve_row(const Proj& P, const PcaData<T>& D
 }
 template <typename T, bool UNFUSED>
 __global__ void __launch_bounds__(PCA_THREADS, 1) k_precond_async(Proj P, PcaData<T> D, T* z, int* status, int lgCS) {
+    grid_dep_wait();
     typedef Pca<T> K;
     if (*P.done) return;
     extern __shared__ __align__(16) unsigned char pca_smem[];
@@ -1461,13 +1484,15 @@ static cudaError_t launch_precond_async(const Dev& d, const Proj& P, const PcaDa
     cfg.blockDim = dim3(PCA_THREADS);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    cudaLaunchAttribute at[1];
+    cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = P.pcCluster;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;  // see launch_pdl
+    at[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 2;
     ++g_launches;
     if (P.unfused) return cudaLaunchKernelEx(&cfg, k_precond_async<T, true>, P, D, z, d.status, log2_exact(P.pcCluster));
     return cudaLaunchKernelEx(&cfg, k_precond_async<T, false>, P, D, z, d.status, log2_exact(P.pcCluster));
@@ -1841,6 +1866,7 @@ __device__ __forceinline__ double mac_add(double acc, double a, double b) {
 }
 template <bool FUSED>
 __global__ void __launch_bounds__(SPMV_THREADS) k_spmv_dot(Proj P, const double* s, double* z, double* part) {
+    grid_dep_wait();
     __shared__ double ys[RED_CHUNK];
     __shared__ double sh[RED_LANES];
     if (*P.done) return;
@@ -1868,6 +1894,7 @@ __global__ void __launch_bounds__(SPMV_THREADS) k_spmv_dot(Proj P, const double*
     if (tl == 0) part[blockIdx.x] = r;
 }
 __global__ void k_alpha(Proj P, const double* part) {
+    grid_dep_wait();
     __shared__ double sh[RED_LANES];
     if (*P.done) return;
     int n = *P.nDof;
@@ -1877,6 +1904,7 @@ __global__ void k_alpha(Proj P, const double* part) {
 }
 template <bool FUSED>
 __global__ void k_update_xr(Proj P, double* x, double* r, const double* s, const double* z) {
+    grid_dep_wait();
     if (*P.done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int n = *P.nDof;
@@ -1893,6 +1921,7 @@ __global__ void k_update_xr(Proj P, double* x, double* r, const double* s, const
     block_absmax_to(v, P.amax);
 }
 __global__ void k_check(Proj P, int maxIter) {
+    grid_dep_wait();
     if (*P.done) return;
     double res = __longlong_as_double((long long)*P.amax);
     *P.amax = 0;
@@ -1911,6 +1940,7 @@ __global__ void k_check(Proj P, int maxIter) {
     }
 }
 __global__ void k_beta(Proj P, const double* part) {
+    grid_dep_wait();
     __shared__ double sh[RED_LANES];
     if (*P.done) return;
     int n = *P.nDof;
@@ -1923,6 +1953,7 @@ __global__ void k_beta(Proj P, const double* part) {
 }
 template <bool FUSED>
 __global__ void k_update_s(Proj P, double* s, const double* z) {
+    grid_dep_wait();
     if (*P.done) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *P.nDof) return;
@@ -2168,20 +2199,20 @@ int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& e
     auto body = [&](int nb, KProf* pf) {
         for (int it = 0; it < nb; ++it) {
             prof_begin(pf, 2, st);
-            if (P.refOrder) ASTG_LAUNCH(k_spmv_dot<false><<<chunks, SPMV_THREADS, 0, st>>>(P, s, z, P.part));
-            else ASTG_LAUNCH(k_spmv_dot<true><<<chunks, SPMV_THREADS, 0, st>>>(P, s, z, P.part));
+            if (P.refOrder) launch_pdl(k_spmv_dot<false>, chunks, SPMV_THREADS, st, P, s, z, P.part);
+            else launch_pdl(k_spmv_dot<true>, chunks, SPMV_THREADS, st, P, s, z, P.part);
             prof_end(pf, st);
             if (P.refOrder) launch_dot_ref(s, z, P.nDof, P.part, st);
-            ASTG_LAUNCH(k_alpha<<<1, RED_LANES, 0, st>>>(P, P.part));
-            if (P.refOrder) ASTG_LAUNCH(k_update_xr<false><<<nblk(maxRows), TB, 0, st>>>(P, x, r, s, z));
-            else ASTG_LAUNCH(k_update_xr<true><<<nblk(maxRows), TB, 0, st>>>(P, x, r, s, z));
-            ASTG_LAUNCH(k_check<<<1, 1, 0, st>>>(P, maxIter));
+            launch_pdl(k_alpha, 1, RED_LANES, st, P, P.part);
+            if (P.refOrder) launch_pdl(k_update_xr<false>, nblk(maxRows), TB, st, P, x, r, s, z);
+            else launch_pdl(k_update_xr<true>, nblk(maxRows), TB, st, P, x, r, s, z);
+            launch_pdl(k_check, 1, 1, st, P, maxIter);
             precond(d, P, r, z, epoch, st, pf);
             if (P.refOrder) launch_dot_ref(z, r, P.nDof, P.part, st);
-            else ASTG_LAUNCH(k_tree_dot<<<chunks, RED_LANES, 0, st>>>(z, r, P.nDof, P.part));
-            ASTG_LAUNCH(k_beta<<<1, RED_LANES, 0, st>>>(P, P.part));
-            if (P.refOrder) ASTG_LAUNCH(k_update_s<false><<<nblk(maxRows), TB, 0, st>>>(P, s, z));
-            else ASTG_LAUNCH(k_update_s<true><<<nblk(maxRows), TB, 0, st>>>(P, s, z));
+            else launch_pdl(k_tree_dot, chunks, RED_LANES, st, z, r, P.nDof, P.part);
+            launch_pdl(k_beta, 1, RED_LANES, st, P, P.part);
+            if (P.refOrder) launch_pdl(k_update_s<false>, nblk(maxRows), TB, st, P, s, z);
+            else launch_pdl(k_update_s<true>, nblk(maxRows), TB, st, P, s, z);
         }
     };
     BatchGraph graph;
