@@ -137,11 +137,13 @@ astg_status astg_set_precision(astg_handle* h, astg_precision prec);
 
 /* Order of the floating-point reductions of the FP64 solve and of addForce's mean temperature.
  * ASTG_ORDER_LIBRARY (the default, the fast path): one fixed reduction tree for every dot product
- * and sum, each sweep update one fused multiply-subtract; results are reproducible, and match the
- * reference to the PCG tolerance.  ASTG_ORDER_REFERENCE: the reference's own arithmetic, so the
+ * and sum, one fused multiply-add for every product the PCG accumulates (sweep updates, matrix
+ * rows, dot terms, vector updates); results are reproducible, and match the reference to the PCG
+ * tolerance.  ASTG_ORDER_REFERENCE: the reference's own arithmetic, so the
  * solve reproduces it bit for bit: dot products in Eigen 3.3.7's SSE2 order (BLAS::dot,
- * include/pcgsolver/blas_wrapper.h:112-115), the MIC(0) sweep updates as a multiply and a
- * subtraction (include/pcgsolver/pcg_solver.h:211-253), and the mean temperature as BLAS::sum's
+ * include/pcgsolver/blas_wrapper.h:112-115), the MIC(0) sweep updates, matrix rows and vector
+ * updates as a multiply and an addition or subtraction (include/pcgsolver/pcg_solver.h:211-253),
+ * and the mean temperature as BLAS::sum's
  * per-worker slice sums (blas_wrapper.h:101-110, include/thread_pool.h:319-348) over `workers`
  * workers, the reference's thread-pool size (its hardware concurrency: the slices depend on it),
  * 1..256.  The reference order runs the dot products and sums as serial chains: it is a parity
