@@ -356,6 +356,9 @@ void build_layout_device(const int32_t* hsplit, int res, int L, const double* ld
         int n = 0;
         lck(cudaMemcpyAsync(&n, total, sizeof(int), cudaMemcpyDeviceToHost, st), "count");
         lck(cudaStreamSynchronize(st), "count");
+        // the fixed reduction tree folds at most 2048 chunk partials in one block (this also keeps
+        // the discovery keys, index * 26 + k, inside int)
+        if (2LL * (off + n) > 2048LL * 2048LL) throw std::runtime_error("layout: too many cells for the reduction tree");
         ASTG_LAUNCH(k_lay_cells<<<lblk(rc), LTB, 0, st>>>(l, r, off, flag, idx, brick, lslot));
         long long keys = (long long)n * 26;
         int g = 0;
