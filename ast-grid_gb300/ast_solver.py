@@ -26,7 +26,7 @@ FP64, MIXED = 0, 1
 
 # exported symbols of include/astg.h
 SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_update",
-           "astg_set_max_cfl", "astg_cfl", "astg_stage", "astg_refine_split_map", "astg_set_collider_sphere",
+           "astg_set_max_cfl", "astg_cfl", "astg_stage", "astg_refine_split_map", "astg_set_collider_sphere", "astg_solve_batch",
            "astg_set_solver_parameters", "astg_set_precision", "astg_set_reduction_order", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
            "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate",
            "astg_restart", "astg_save_checkpoint", "astg_tape_start", "astg_tape_stop", "astg_adjoint_reset",
@@ -114,6 +114,8 @@ def lib(path=None):
         L.astg_set.argtypes = [c_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t]
         L.astg_solve.argtypes = [c_p, ctypes.c_int, c_p, c_p, c_p, c_p, c_p, ctypes.c_double, ctypes.c_int,
                                  ctypes.c_int, ctypes.POINTER(SolveStats)]
+        L.astg_solve_batch.argtypes = [c_p, ctypes.c_int, c_p, c_p, c_p, ctypes.c_int, c_p, c_p, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_int, ctypes.POINTER(SolveStats), c_p, c_p]
         L.astg_max_velocity.argtypes = [c_p, ctypes.POINTER(ctypes.c_double)]
         L.astg_restart.argtypes = [c_p, ctypes.c_int] + [ctypes.c_char_p] * 6
         L.astg_save_checkpoint.argtypes = [c_p] + [ctypes.c_char_p] * 5
@@ -425,6 +427,27 @@ class OctreeSmoke3:
                                      x.ctypes.data, rel_tol, max_iter, prec, ctypes.byref(st)),
                     allow=(ASTG_NOT_CONVERGED,))
         return x, st
+
+    def solve_batch(self, rowptr, col, val, B, rel_tol=1e-6, max_iter=3000, precision="fp64"):
+        """astg_solve for every row of B (nrhs x n) on one matrix, the solves side by side on the
+        device; returns (X, [SolveStats], wall_ms, lanes).  Each row of X is what solve() returns."""
+        rp = np.ascontiguousarray(rowptr, dtype=np.int32)
+        c = np.ascontiguousarray(col, dtype=np.int32)
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        bb = np.ascontiguousarray(B, dtype=np.float64)
+        if bb.ndim != 2:
+            raise ValueError("B must be nrhs x n")
+        nrhs, n = bb.shape
+        x = np.zeros((nrhs, n))
+        st = (SolveStats * nrhs)()
+        wall = ctypes.c_double(0)
+        lanes = ctypes.c_int(0)
+        prec = {"fp64": FP64, "mixed": MIXED}.get(precision, precision)
+        self._check(lib().astg_solve_batch(self._h, n, rp.ctypes.data, c.ctypes.data, v.ctypes.data, nrhs,
+                                           bb.ctypes.data, x.ctypes.data, rel_tol, max_iter, prec, st,
+                                           ctypes.byref(wall), ctypes.byref(lanes)),
+                    allow=(ASTG_NOT_CONVERGED,))
+        return x, list(st), wall.value, lanes.value
 
     def extrapolate(self, field, sdf, valid_offset=0.0, max_distance_factor=4.0):
         """FmmLevelSetSolver3::extrapolate (include/jet/fmm_levelset_solver3.h:84-408) of "density"

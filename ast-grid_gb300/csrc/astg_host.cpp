@@ -4,6 +4,10 @@
 // include/astg.h.  All per-step work runs on the GPU; the host only launches and, for the
 // PCG's stopping test and the status word, reads a few bytes back.
 #include <algorithm>
+#include <chrono>
+#include <exception>
+#include <thread>
+#include <utility>
 #include <cmath>
 #include <limits>
 #include <cstdarg>
@@ -124,6 +128,7 @@ struct astg_handle {
 
     ~astg_handle() {
         if (st) cudaStreamSynchronize(st);
+        freeLanes();
         freeTape();
         for (void* p : allocs) cudaFree(p);
         if (J.hostDone) cudaFreeHost(J.hostDone);
@@ -869,6 +874,189 @@ struct astg_handle {
         ck(cudaStreamSynchronize(st), "solve");
         if (stats) *stats = last;
     }
+
+    // ---- several right-hand sides of one matrix (astg_solve_batch).  The matrix, its MIC(0) factor
+    // and the level schedule are computed once and shared; each lane owns the PCG's vectors and
+    // scalars and a stream and runs the launches astg_solve runs, so every solution is the one
+    // astg_solve returns, bit for bit.  A solve keeps one 16-CTA cluster busy in its
+    // preconditioner, so lanes on other SMs use the GPU that a single solve leaves idle; lanes are
+    // driven by one host thread each.
+    struct Lane {
+        double *b = nullptr, *x = nullptr, *r = nullptr, *s = nullptr, *z = nullptr, *part = nullptr, *sc = nullptr;
+        double *rl = nullptr, *yl = nullptr;
+        float *rl32 = nullptr, *yl32 = nullptr, *e32 = nullptr, *r32 = nullptr, *s32 = nullptr, *z32 = nullptr,
+              *q32 = nullptr;
+        int *isc = nullptr, *done = nullptr, *hostDone = nullptr;
+        unsigned long long* amax = nullptr;
+        cudaStream_t st = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+    };
+    std::vector<Lane> lanes;
+    void ensureLanes(int k) {
+        const size_t rows = J.rowsCap;
+        while ((int)lanes.size() < k) {
+            Lane L;
+            L.b = dalloc<double>(rows); L.x = dalloc<double>(rows); L.r = dalloc<double>(rows);
+            L.s = dalloc<double>(rows); L.z = dalloc<double>(rows);
+            L.part = dalloc<double>((rows + 2047) / 2048 + 1);
+            L.sc = dalloc<double>(SC_COUNT);
+            L.isc = dalloc<int>(ISC_COUNT);
+            L.amax = dalloc<unsigned long long>(1);
+            L.done = dalloc<int>(1);
+            if (J.rl) L.rl = dalloc<double>(rows);
+            if (J.yl) L.yl = dalloc<double>(rows);
+            if (J.rl32) {
+                L.rl32 = dalloc<float>(rows); L.yl32 = dalloc<float>(rows); L.e32 = dalloc<float>(rows);
+                L.r32 = dalloc<float>(rows); L.s32 = dalloc<float>(rows); L.z32 = dalloc<float>(rows);
+                L.q32 = dalloc<float>(rows);
+            }
+            lanes.push_back(L);  // owned from here on: the destructor releases what follows
+            Lane& M = lanes.back();
+            ck(cudaMallocHost(&M.hostDone, sizeof(int)), "cudaMallocHost");
+            ck(cudaStreamCreateWithFlags(&M.st, cudaStreamNonBlocking), "stream");
+            ck(cudaEventCreate(&M.e0), "event");
+            ck(cudaEventCreate(&M.e1), "event");
+        }
+    }
+    void freeLanes() {
+        for (Lane& L : lanes) {
+            if (L.st) cudaStreamSynchronize(L.st);
+            if (L.e0) cudaEventDestroy(L.e0);
+            if (L.e1) cudaEventDestroy(L.e1);
+            if (L.st) cudaStreamDestroy(L.st);
+            if (L.hostDone) cudaFreeHost(L.hostDone);
+        }
+        lanes.clear();
+    }
+    // the handle's workspace with lane L's vectors and scalars
+    Proj laneView(const Lane& L) const {
+        Proj Q = J;
+        Q.b = L.b; Q.x = L.x; Q.r = L.r; Q.s = L.s; Q.z = L.z; Q.part = L.part; Q.sc = L.sc; Q.isc = L.isc;
+        Q.amax = L.amax; Q.done = L.done; Q.hostDone = L.hostDone;
+        Q.rl = L.rl; Q.yl = L.yl;
+        Q.rl32 = L.rl32; Q.yl32 = L.yl32; Q.e32 = L.e32; Q.r32 = L.r32; Q.s32 = L.s32; Q.z32 = L.z32; Q.q32 = L.q32;
+        return Q;
+    }
+    void solveBatch(int n, const int32_t* rowptr, const int32_t* col, const double* val, int nrhs, const double* B,
+                    double* X, double tol, int maxIter, int precision, astg_solve_stats* stats, double* wallMs) {
+        long long rows = J.rowsCap;
+        if (nrhs <= 0) throw std::invalid_argument("astg_solve_batch: nrhs must be positive");
+        if (n <= 0 || n > rows)
+            throw std::invalid_argument("astg_solve_batch: n exceeds the handle's capacity (2 x cells + half tilts)");
+        long long nnz = rowptr[n];
+        if (nnz <= 0 || nnz > rows * ROW_W) throw std::invalid_argument("astg_solve_batch: too many non-zeros for the workspace");
+        for (int i = 0; i < n; ++i)
+            if (rowptr[i + 1] - rowptr[i] > ROW_W || rowptr[i + 1] < rowptr[i])
+                throw std::invalid_argument("astg_solve_batch: malformed row pointer or row longer than 32 entries");
+        const auto t0 = std::chrono::steady_clock::now();
+        int nn = n, nz = (int)nnz;
+        ck(cudaMemcpyAsync(J.nDof, &nn, sizeof(int), cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaMemcpyAsync(J.nnz, &nz, sizeof(int), cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaMemcpyAsync(J.rowPtr, rowptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaMemcpyAsync(J.col, col, sizeof(int) * nnz, cudaMemcpyHostToDevice, st), "upload");
+        ck(cudaMemcpyAsync(J.val, val, sizeof(double) * nnz, cudaMemcpyHostToDevice, st), "upload");
+        select_preconditioner(J, n);
+        launch_external_system(d, J, n, st);
+        checkStatus();
+        const bool mixed = precision == ASTG_MIXED && J.pcActive32;
+        launch_factor(d, J, P.omega, P.min_diag, epoch, st, nullptr);
+        const bool owner = mixed || (J.pcActive && J.pcAsync);
+        if (J.clusterSize > 0 || J.pcActive || mixed) launch_level_schedule(d, J, owner, st);
+        ck(cudaStreamSynchronize(st), "factor");
+        checkStatus();
+        // lanes only with the barrier-free preconditioner: the other forms hand rows out from one
+        // counter and epoch flags of the handle
+        const bool concurrent = mixed || (J.pcActive && J.pcAsync);
+        const int k = concurrent ? std::min(nrhs, precond_concurrency(J, mixed)) : 0;
+        auto record = [&](int i, int outer, const int* isc, const double* sc, float ms) {
+            astg_solve_stats o{};
+            o.iterations = isc[ISC_ITERS];
+            o.converged = isc[ISC_CONVERGED];
+            o.outer = outer;
+            o.n = n;
+            o.nnz = (int)nnz;
+            o.residual = sc[SC_RESID];
+            o.tolerance = sc[SC_TOL];
+            o.ms = ms;
+            if (stats) stats[i] = o;
+            last = o;
+        };
+        if (k == 0) {  // one after another on the handle's own workspace
+            for (int i = 0; i < nrhs; ++i) {
+                ck(cudaMemcpyAsync(J.b, B + (size_t)i * n, sizeof(double) * n, cudaMemcpyHostToDevice, st), "upload");
+                ck(cudaEventRecord(evA, st), "event");
+                int outer = 0;
+                if (mixed) outer = launch_pcg_mixed(d, J, tol, maxIter, 8, st, nullptr);
+                else launch_pcg_fp64(d, J, tol, maxIter, epoch, 8, st, nullptr);
+                ck(cudaEventRecord(evB, st), "event");
+                ck(cudaMemcpyAsync(X + (size_t)i * n, J.x, sizeof(double) * n, cudaMemcpyDeviceToHost, st), "download");
+                int isc[ISC_COUNT];
+                double sc[SC_COUNT];
+                ck(cudaMemcpyAsync(isc, J.isc, sizeof isc, cudaMemcpyDeviceToHost, st), "stats");
+                ck(cudaMemcpyAsync(sc, J.sc, sizeof sc, cudaMemcpyDeviceToHost, st), "stats");
+                ck(cudaStreamSynchronize(st), "solve");
+                float ms = 0;
+                cudaEventElapsedTime(&ms, evA, evB);
+                record(i, outer, isc, sc, ms);
+            }
+        } else {
+            ensureLanes(k);
+            std::vector<std::exception_ptr> errs(k);
+            std::vector<std::vector<std::pair<int, std::vector<double>>>> out(k);
+            std::vector<std::thread> th;
+            for (int w = 0; w < k; ++w)
+                th.emplace_back([&, w] {
+                    try {
+                        ck(cudaSetDevice(P.device), "cudaSetDevice");
+                        Lane& L = lanes[w];
+                        Proj Q = laneView(L);
+                        int ep = 0;  // the barrier-free forms use no epoch flags
+                        for (int i = w; i < nrhs; i += k) {
+                            ck(cudaMemcpyAsync(Q.b, B + (size_t)i * n, sizeof(double) * n, cudaMemcpyHostToDevice, L.st), "upload");
+                            ck(cudaEventRecord(L.e0, L.st), "event");
+                            int outer = 0;
+                            if (mixed) outer = launch_pcg_mixed(d, Q, tol, maxIter, 8, L.st, nullptr);
+                            else launch_pcg_fp64(d, Q, tol, maxIter, ep, 8, L.st, nullptr);
+                            ck(cudaEventRecord(L.e1, L.st), "event");
+                            ck(cudaMemcpyAsync(X + (size_t)i * n, Q.x, sizeof(double) * n, cudaMemcpyDeviceToHost, L.st), "download");
+                            int isc[ISC_COUNT];
+                            double sc[SC_COUNT];
+                            ck(cudaMemcpyAsync(isc, Q.isc, sizeof isc, cudaMemcpyDeviceToHost, L.st), "stats");
+                            ck(cudaMemcpyAsync(sc, Q.sc, sizeof sc, cudaMemcpyDeviceToHost, L.st), "stats");
+                            ck(cudaStreamSynchronize(L.st), "solve");
+                            float ms = 0;
+                            cudaEventElapsedTime(&ms, L.e0, L.e1);
+                            out[w].push_back({i, {(double)isc[ISC_ITERS], (double)isc[ISC_CONVERGED], (double)outer,
+                                                  sc[SC_RESID], sc[SC_TOL], (double)ms}});
+                        }
+                    } catch (...) {
+                        errs[w] = std::current_exception();
+                    }
+                });
+            for (auto& t : th) t.join();
+            for (auto& e : errs)
+                if (e) std::rethrow_exception(e);
+            for (int w = 0; w < k; ++w)
+                for (auto& rec : out[w]) {
+                    const std::vector<double>& v = rec.second;
+                    int isc[ISC_COUNT] = {(int)v[0], (int)v[1]};
+                    double sc[SC_COUNT] = {};
+                    sc[SC_RESID] = v[3];
+                    sc[SC_TOL] = v[4];
+                    record(rec.first, (int)v[2], isc, sc, (float)v[5]);
+                }
+        }
+        if (g_cluster_error != cudaSuccess) {
+            cudaError_t e = g_cluster_error;
+            g_cluster_error = cudaSuccess;
+            ck(e, "cluster sweep launch");
+        }
+        checkStatus();
+        lastLanes = std::max(k, 1);
+        if (wallMs)
+            *wallMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    int lastLanes = 1;
 
     void stage(int id, double dt) {
         Fields& C = F[cur];
@@ -1907,6 +2095,23 @@ astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32
     if (prec != ASTG_FP64 && prec != ASTG_MIXED) return ASTG_BAD_ARG;
     astg_status s = guard(h, [&] { h->solveExternal(n, rowptr, col, val, b, x, rel_tol, max_iter, prec, stats); });
     if (s == ASTG_OK && !h->last.converged) return ASTG_NOT_CONVERGED;
+    return s;
+}
+
+astg_status astg_solve_batch(astg_handle* h, int n, const int32_t* rowptr, const int32_t* col, const double* val,
+                             int nrhs, const double* b, double* x, double rel_tol, int max_iter, astg_precision prec,
+                             astg_solve_stats* stats, double* wall_ms, int* lanes) {
+    if (!h || !rowptr || !col || !val || !b || !x || max_iter <= 0 || nrhs <= 0) return ASTG_BAD_ARG;
+    if (prec != ASTG_FP64 && prec != ASTG_MIXED) return ASTG_BAD_ARG;
+    bool all = true;
+    astg_status s = guard(h, [&] {
+        std::vector<astg_solve_stats> st(nrhs);
+        h->solveBatch(n, rowptr, col, val, nrhs, b, x, rel_tol, max_iter, prec, st.data(), wall_ms);
+        for (int i = 0; i < nrhs; ++i) all = all && st[i].converged;
+        if (stats) std::copy(st.begin(), st.end(), stats);
+        if (lanes) *lanes = h->lastLanes;
+    });
+    if (s == ASTG_OK && !all) return ASTG_NOT_CONVERGED;
     return s;
 }
 

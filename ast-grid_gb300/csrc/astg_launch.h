@@ -10,9 +10,15 @@ namespace astg {
 // number of kernels this library has launched (all handles of the process; calls on several host
 // threads may count at once)
 extern std::atomic<long long> g_launches;
+// the calling thread's launches (a graph capture counts the kernels of its own thread only)
+extern thread_local long long t_launches;
+inline void count_launch() {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    ++t_launches;
+}
 #define ASTG_LAUNCH(...)                                                       \
     do {                                                                       \
-        ::astg::g_launches.fetch_add(1, std::memory_order_relaxed);            \
+        ::astg::count_launch();                                                \
         __VA_ARGS__;                                                           \
     } while (0)
 
@@ -267,6 +273,8 @@ int launch_pcg_fp64(const Dev& d, Proj& P, double tolFactor, int maxIter, int& e
 // mixed-precision PCG (FP32 inner PCG inside FP64 defect correction); returns the outer cycles, or
 // -1 when the FP32 preconditioner is not available for this solve (nothing was run)
 int launch_pcg_mixed(const Dev& d, Proj& P, double tolFactor, int maxIter, int batch, cudaStream_t st, KProf* prof);
+// clusters of the barrier-free preconditioner that fit on the device at once (1..8)
+int precond_concurrency(const Proj& P, bool fp32);
 void launch_pressure_update(const Dev& d, const Fields& F, const uint8_t* open, const int* pO, const int* pT,
                             const double* p, double dt, cudaStream_t st);
 void launch_dual(const Dev& d, const Fields& F, cudaStream_t st);

@@ -45,6 +45,7 @@ namespace cg = cooperative_groups;
 namespace astg {
 
 std::atomic<long long> g_launches{0};
+thread_local long long t_launches = 0;
 
 // event pairs around profiled launches; drained after each host synchronisation.  On a capturing
 // stream the records become event-record nodes of the graph (external records) in a separate set
@@ -125,7 +126,7 @@ struct BatchGraph {
         const int k = (prof && prof->on && replays % KPROF_GRAPH_EVERY == 0) ? 1 : 0;
         if (!exec[k]) {
             if (k) prof->gused = 0;
-            long long l0 = g_launches;
+            long long l0 = t_launches;
             if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
                 cudaGetLastError();
                 failed = true;
@@ -136,8 +137,9 @@ struct BatchGraph {
             cudaError_t e = cudaStreamEndCapture(st, &g);
             if (e == cudaSuccess) e = cudaGraphInstantiate(&exec[k], g, 0);
             if (g) cudaGraphDestroy(g);
-            launches[k] = g_launches.load() - l0;
+            launches[k] = t_launches - l0;
             g_launches -= launches[k];  // captured, not launched: counted at each replay
+            t_launches -= launches[k];
             if (e != cudaSuccess) {
                 cudaGetLastError();
                 exec[k] = nullptr;
@@ -151,6 +153,7 @@ struct BatchGraph {
             return false;
         }
         g_launches += launches[k];
+        t_launches += launches[k];
         ++replays;
         profiled = k == 1;
         return true;
@@ -195,7 +198,7 @@ static void launch_pdl(void (*k)(KArgs...), int grid, int block, cudaStream_t st
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    ++g_launches;
+    count_launch();
     cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
 }
 
@@ -482,13 +485,13 @@ cudaError_t launch_mean_temperature_static(const double* heat, const LevelSpans&
     LevelSpans spv = sp;
     if (m > 0) {
         void* args[] = {(void*)&heat, (void*)&spv, (void*)&parts};
-        ++g_launches;
+        count_launch();
         e = cudaLaunchKernel((const void*)k_tree_sum_levels, dim3(m), dim3(RED_LANES), args, 0, st);
         if (e != cudaSuccess) return e;
     }
     const double* pc = parts;
     void* args2[] = {(void*)&spv, (void*)&pc, (void*)&amb};
-    ++g_launches;
+    count_launch();
     return cudaLaunchKernel((const void*)k_amb_levels, dim3(1), dim3(RED_LANES), args2, 0, st);
 }
 
@@ -1459,6 +1462,29 @@ __global__ void __launch_bounds__(PCA_THREADS, 1) k_precond_async(Proj P, PcaDat
         if (j < n) z[j] = zsh[l];
     }
 }
+// how many clusters of the barrier-free preconditioner (FP64 or FP32 form) can be resident at
+// once, at most 8: the number of solves that can run side by side on disjoint SMs
+int precond_concurrency(const Proj& P, bool fp32) {
+    if (P.pcCluster <= 0) return 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(P.pcCluster);
+    cfg.blockDim = dim3(PCA_THREADS);
+    cfg.dynamicSmemBytes = fp32 ? P.pcSmem32 : P.pcSmem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = P.pcCluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const void* k = fp32 ? (const void*)k_precond_async<float, false> : (const void*)k_precond_async<double, false>;
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, k, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        nc = 1;
+    }
+    return std::max(1, std::min(nc, 8));
+}
 static cudaError_t launch_precond_dsmem(const Proj& P, const double* r, double* z, cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(P.pcCluster);
@@ -1472,7 +1498,7 @@ static cudaError_t launch_precond_dsmem(const Proj& P, const double* r, double* 
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    ++g_launches;
+    count_launch();
     (void)r;
     return cudaLaunchKernelEx(&cfg, k_precond_dsmem, P, z, log2_exact(P.pcCluster));
 }
@@ -1493,7 +1519,7 @@ static cudaError_t launch_precond_async(const Dev& d, const Proj& P, const PcaDa
     at[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 2;
-    ++g_launches;
+    count_launch();
     if (P.unfused) return cudaLaunchKernelEx(&cfg, k_precond_async<T, true>, P, D, z, d.status, log2_exact(P.pcCluster));
     return cudaLaunchKernelEx(&cfg, k_precond_async<T, false>, P, D, z, d.status, log2_exact(P.pcCluster));
 }
@@ -1575,7 +1601,7 @@ static cudaError_t launch_cluster(void (*kern)(Proj, const double*, double*), in
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    ++g_launches;
+    count_launch();
     return cudaLaunchKernelEx(&cfg, kern, P, r, z);
 }
 // largest cluster size (16, 8, 4, 2) that can be resident for the sweep kernels

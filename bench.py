@@ -192,6 +192,7 @@ def isolated_solves(args, device):
     snap = {k: s.get(k) for k in fields + ["t_" + k for k in fields] + ["tilt_open"]}
     S = s.slots
     out = {"fp64": [], "mixed": []}
+    rhs, sols = [], {"fp64": [], "mixed": []}
     A = None
     for k in range(args.solve_rhs):
         rng = np.random.default_rng(1 + k)
@@ -212,9 +213,11 @@ def isolated_solves(args, device):
         for _ in range(3):
             ax = np.add.reduceat(val * b[col], rp[:-1])
             b = (1 - 2 / 3.0) * b + (2 / 3.0) * (0.0 - (ax - diag * b)) / diag
+        rhs.append(b)
         for prec in ("fp64", "mixed"):
-            _, st = s.solve(rp, col, val, b, rel_tol=1e-6, precision=prec)
+            x, st = s.solve(rp, col, val, b, rel_tol=1e-6, precision=prec)
             out[prec].append((st.ms, st.iterations, st.outer, st.converged))
+            sols[prec].append(x)
     rp, col, val = A
     n, nnz = len(rp) - 1, len(col)
     nnzL = (nnz - n) / 2
@@ -232,6 +235,17 @@ def isolated_solves(args, device):
         res[prec] = {"ms_per_solve": ms, "iterations_mean": it, "outer_cycles_mean": outer,
                      "all_converged": all(r[3] == 1 for r in rows_), "algorithmic_GBps": bytes_ / (ms / 1e3) / 1e9}
     res["mixed_speedup"] = res["fp64"]["ms_per_solve"] / res["mixed"]["ms_per_solve"]
+    # the same right-hand sides through astg_solve_batch: the solves side by side, one preconditioner
+    # cluster each (host wall time of the whole call per right-hand side, factorisation and copies
+    # included); the solutions must equal the one-by-one ones bit for bit
+    if rhs:
+        B = np.stack(rhs)
+        for prec in ("fp64", "mixed"):
+            s.solve_batch(rp, col, val, B[:2], rel_tol=1e-6, precision=prec)  # lanes allocated, warm
+            X, stb, wall, lanes = s.solve_batch(rp, col, val, B, rel_tol=1e-6, precision=prec)
+            same = all(np.array_equal(X[i], sols[prec][i]) for i in range(len(rhs)))
+            res[prec]["batch"] = {"ms_per_solve": wall / len(rhs), "lanes": lanes, "identical": bool(same),
+                                  "all_converged": all(st.converged == 1 for st in stb)}
     s.close()
     return res
 
@@ -656,6 +670,10 @@ def compact_line(full, detail_path):
         line["solves"] = {"fp64_ms": _r(iso["fp64"]["ms_per_solve"], 4), "mixed_ms": _r(iso["mixed"]["ms_per_solve"], 4),
                           "fp64_it": _r(iso["fp64"]["iterations_mean"], 4),
                           "mixed_it": _r(iso["mixed"]["iterations_mean"], 4), "speedup": _r(iso["mixed_speedup"], 3)}
+        if "batch" in iso["fp64"]:
+            line["solves"]["batch_fp64_ms"] = _r(iso["fp64"]["batch"]["ms_per_solve"], 4)
+            line["solves"]["batch_mixed_ms"] = _r(iso["mixed"]["batch"]["ms_per_solve"], 4)
+            line["solves"]["lanes"] = iso["fp64"]["batch"]["lanes"]
     adj = full.get("adjoint")
     if adj:
         line["adjoint"] = {"ratio": _r(adj["adjoint_fwd_cost_ratio"], 3),

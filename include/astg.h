@@ -197,6 +197,16 @@ astg_status astg_solve(astg_handle* h, int n, const int32_t* rowptr, const int32
                        const double* b, double* x, double rel_tol, int max_iter, astg_precision prec,
                        astg_solve_stats* stats);
 
+/* astg_solve for nrhs right-hand sides of one matrix (b and x: nrhs rows of n values).  The
+ * factorisation is computed once; the solves run side by side (each keeps one cluster of the
+ * preconditioner busy, and up to 8 clusters fit on the device), each returning the result astg_solve
+ * returns for its right-hand side, bit for bit.  stats (nrhs entries), wall_ms (host time of the whole
+ * call, copies included) and lanes (solves run side by side) may be NULL.  No counterpart in the
+ * reference, which solves one right-hand side per PCGSolver::solve call. */
+astg_status astg_solve_batch(astg_handle* h, int n, const int32_t* rowptr, const int32_t* col, const double* val,
+                             int nrhs, const double* b, double* x, double rel_tol, int max_iter, astg_precision prec,
+                             astg_solve_stats* stats, double* wall_ms, int* lanes);
+
 /* Largest MAC face value over all faces, starting from 0 (signed, as the reference's max(v)),
  * the quantity OctreeOmniGridSolver3::cfl divides by the finest spacing
  * (src/octree_omnigrid_solver3.cpp:1066-1122). */
