@@ -60,9 +60,13 @@ def _fake_full():
             "gpu_launches": 61234,
             "isolated_solves": {"config": "x" * 150, "n": 372862, "nnz": 2634386,
                                 "fp64": {"ms_per_solve": 90.51234, "iterations_mean": 164.35, "outer_cycles_mean": 1.0,
-                                         "all_converged": True, "algorithmic_GBps": 120.123},
+                                         "all_converged": True, "algorithmic_GBps": 120.123,
+                                         "batch": {"ms_per_solve": 17.4234567, "lanes": 7, "identical": True,
+                                                   "all_converged": True}},
                                 "mixed": {"ms_per_solve": 75.51234, "iterations_mean": 175.1, "outer_cycles_mean": 2.0,
-                                          "all_converged": True, "algorithmic_GBps": 130.123},
+                                          "all_converged": True, "algorithmic_GBps": 130.123,
+                                          "batch": {"ms_per_solve": 14.8234567, "lanes": 8, "identical": True,
+                                                    "all_converged": True}},
                                 "mixed_speedup": 1.1987654},
             "adjoint": {"config": "x" * 200, "slots": 40000, "mixed": {"ratio": 2.0612345}, "fp64": {"ratio": 2.1},
                         "adjoint_fwd_cost_ratio": 2.0612345, "grad_rel_error_mixed_vs_fp64": 3.0123456e-05,
@@ -72,6 +76,8 @@ def _fake_full():
                                      "rel_residual_mixed": pick, "per_step_density": series,
                                      "per_step_pressure": series, "per_step_divergence_fp64": series,
                                      "per_step_divergence_mixed": series},
+            "ensemble": {"simulations": 7, "steps_each": 10, "wall_s": 1.2345678, "aggregate_steps_per_s": 56.789012345,
+                         "steps_per_s_each": 8.1234567, "member_identical_to_alone": True, "note": "x" * 80},
             "uniform2d": {"workload": "x" * 80, "value": 3.310806460212116, "unit": "frames/s",
                           "ms_per_frame": 302.04121322631835, "e2e": {"value": 3.3}, "cpu_baseline": {"value": 1.4}}}
 
