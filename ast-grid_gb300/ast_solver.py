@@ -26,7 +26,7 @@ FP64, MIXED = 0, 1
 
 # exported symbols of include/astg.h
 SYMBOLS = ["astg_default_params", "astg_create", "astg_destroy", "astg_last_error", "astg_step", "astg_update",
-           "astg_set_max_cfl", "astg_cfl", "astg_stage", "astg_refine_split_map", "astg_set_collider_sphere", "astg_solve_batch",
+           "astg_set_max_cfl", "astg_cfl", "astg_stage", "astg_refine_split_map", "astg_set_collider_sphere", "astg_solve_batch", "astg_refine_split_map_device",
            "astg_set_solver_parameters", "astg_set_precision", "astg_set_reduction_order", "astg_set_profiling", "astg_last_solve", "astg_size", "astg_get", "astg_set",
            "astg_solve", "astg_max_velocity", "astg_mean_temperature_noalloc", "astg_extrapolate",
            "astg_restart", "astg_save_checkpoint", "astg_tape_start", "astg_tape_stop", "astg_adjoint_reset",
@@ -102,6 +102,8 @@ def lib(path=None):
         L.astg_set_precision.argtypes = [c_p, ctypes.c_int]
         L.astg_update.argtypes = [c_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(StepStats)]
         L.astg_set_max_cfl.argtypes = [c_p, ctypes.c_double]
+        L.astg_refine_split_map_device.argtypes = [c_p, ctypes.c_int, ctypes.c_int, c_p, ctypes.c_double,
+                                                   ctypes.c_double, c_p]
         L.astg_set_collider_sphere.argtypes = [c_p, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.astg_refine_split_map.argtypes = [c_p, ctypes.c_int, ctypes.c_int, c_p, ctypes.c_double, ctypes.c_double]
         L.astg_cfl.argtypes = [c_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
@@ -197,6 +199,27 @@ def refine_split_map(split_map, level, sdf, split_range):
     if st != ASTG_OK:
         raise AstgError(st, "resolution not divisible by 2^level, or a bad argument")
     return sm.reshape(np.shape(split_map))
+
+
+def refine_split_map_tensor(split_map, level, sdf, split_range):
+    """refine_split_map on CUDA tensors (int32 and float64, res^3 elements each, contiguous), in place
+    on the tensors' device and current stream (astg_refine_split_map_device)."""
+    import torch
+
+    if not (split_map.is_cuda and sdf.is_cuda) or split_map.dtype != torch.int32 or sdf.dtype != torch.float64:
+        raise ValueError("refine_split_map_tensor: int32 and float64 CUDA tensors")
+    if not (split_map.is_contiguous() and sdf.is_contiguous()) or split_map.numel() != sdf.numel():
+        raise ValueError("refine_split_map_tensor: contiguous tensors of res^3 elements")
+    res = round(split_map.numel() ** (1 / 3))
+    if res ** 3 != split_map.numel():
+        raise ValueError("refine_split_map_tensor: res^3 elements")
+    stream = torch.cuda.current_stream(split_map.device).cuda_stream
+    with torch.cuda.device(split_map.device):
+        st = lib().astg_refine_split_map_device(split_map.data_ptr(), res, int(level), sdf.data_ptr(),
+                                                float(split_range[0]), float(split_range[1]), stream)
+    if st != ASTG_OK:
+        raise AstgError(st, "resolution not divisible by 2^level, host memory, or a failed launch")
+    return split_map
 
 
 class OctreeSmoke3:

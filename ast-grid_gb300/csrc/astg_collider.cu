@@ -219,6 +219,33 @@ void launch_collider_sphere_sdf(int res, double cx, double cy, double cz, double
     ASTG_LAUNCH(k_col_sphere_sdf<<<(unsigned)((n + CTB - 1) / CTB), CTB, 0, st>>>(res, 1.0 / res, cx, cy, cz, r, sdf));
 }
 
+// refineSplitMapByObstacleSdf (include/octree_util.h:17-47) on device arrays: one thread per block
+// of 2^level finest cells; a block whose corner cell carries split value `level` and whose SDF,
+// sampled at the block centre, lies in [lo, hi] is set to level - 1.  Blocks read and write only
+// their own cells, as in the reference's parallel loop.
+__global__ void k_refine_split(int32_t* split, int res, int level, const double* sdf, double lo, double hi) {
+    const long long c = res >> level;
+    long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= c * c * c) return;
+    const int tx = (int)(t % c), ty = (int)((t / c) % c), tz = (int)(t / (c * c));
+    auto at = [&](int x, int y, int z) -> int32_t& { return split[((size_t)z * res + y) * res + x]; };
+    if (at(tx << level, ty << level, tz << level) != level) return;
+    const double dh = (1.0 / res) * (1 << level);
+    const double v = sdf_sample(sdf, res, v3((tx + 0.5) * dh, (ty + 0.5) * dh, (tz + 0.5) * dh));
+    if (!(v >= lo && v <= hi)) return;
+    const int k = 1 << level;
+    for (int z = tz << level; z < (tz << level) + k; ++z)
+        for (int y = ty << level; y < (ty << level) + k; ++y)
+            for (int x = tx << level; x < (tx << level) + k; ++x) at(x, y, z) = level - 1;
+}
+cudaError_t launch_refine_split_map(int32_t* split, int res, int level, const double* sdf, double lo, double hi,
+                                    cudaStream_t st) {
+    const long long c = res >> level, n = c * c * c;
+    void* args[] = {&split, &res, &level, &sdf, &lo, &hi};
+    count_launch();
+    return cudaLaunchKernel((const void*)k_refine_split, dim3((unsigned)((n + CTB - 1) / CTB)), dim3(CTB), args, 0, st);
+}
+
 // halfDir: each half tilt's direction (0-5, the list order of d.half)
 void launch_collider_setup(const Dev& d, const int* halfDir, uint16_t* mask, double* wMac, double* wTilt,
                            cudaStream_t st) {

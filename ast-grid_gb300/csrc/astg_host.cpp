@@ -2014,6 +2014,26 @@ astg_status astg_refine_split_map(int32_t* split_map, int res, int level, const 
     return ASTG_OK;
 }
 
+astg_status astg_refine_split_map_device(int32_t* d_split_map, int res, int level, const double* d_sdf, double lo,
+                                         double hi, void* stream) {
+    if (!d_split_map || !d_sdf || res <= 0 || level < 1 || level > 30) return ASTG_BAD_ARG;
+    if (res % (1 << level) != 0) return ASTG_BAD_ARG;  // "resolution is not dividable by level"
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return ASTG_CUDA_ERROR;
+    const void* ptrs[2] = {d_split_map, d_sdf};
+    for (const void* q : ptrs) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();
+            return ASTG_BAD_ARG;
+        }
+        bool onDevice = a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+        if (!onDevice || (a.type == cudaMemoryTypeDevice && a.device != dev)) return ASTG_BAD_ARG;
+    }
+    cudaError_t e = launch_refine_split_map(d_split_map, res, level, d_sdf, lo, hi, (cudaStream_t)stream);
+    return e == cudaSuccess ? ASTG_OK : ASTG_CUDA_ERROR;
+}
+
 astg_status astg_update(astg_handle* h, double dt, int* substeps, astg_step_stats* stats) {
     if (!h || !(dt >= 0)) return ASTG_BAD_ARG;
     astg_status s = guard(h, [&] { h->update(dt, substeps, stats); });

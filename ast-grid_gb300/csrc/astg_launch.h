@@ -229,6 +229,9 @@ void build_layout_device(const int32_t* split, int res, int L, const double* ldh
 // out = exclusive scan of in[0..n), *total = the sum; bsum holds ceil(n / 1024) ints
 void exclusive_scan(const int* in, int* out, int* bsum, int* total, long long n, cudaStream_t st);
 
+// refineSplitMapByObstacleSdf on device arrays; the launch's own error, the thread's error state untouched
+cudaError_t launch_refine_split_map(int32_t* split, int res, int level, const double* sdf, double lo, double hi,
+                                    cudaStream_t st);
 // the SDF grid of a sphere collider at the finest cell centres (res^3 doubles)
 void launch_collider_sphere_sdf(int res, double cx, double cy, double cz, double r, double* sdf, cudaStream_t st);
 void launch_collider_setup(const Dev& d, const int* halfDir, uint16_t* mask, double* wMac, double* wTilt,

@@ -87,6 +87,12 @@ typedef struct astg_step_stats {
  * sdf are res^3 arrays (index (z * res + y) * res + x; sdf at the finest cell centres, inside the
  * obstacle negative).  ASTG_BAD_ARG when res is not divisible by 2^level.  Needs no device. */
 astg_status astg_refine_split_map(int32_t* split_map, int res, int level, const double* sdf, double lo, double hi);
+/* The same on device memory of the current device (split_map and sdf device pointers), one thread
+ * per block on `stream` (a cudaStream_t; NULL: the default stream), asynchronous; the result equals
+ * astg_refine_split_map's.  ASTG_BAD_ARG for host pointers or bad sizes, ASTG_CUDA_ERROR when the
+ * launch fails. */
+astg_status astg_refine_split_map_device(int32_t* split_map, int res, int level, const double* sdf, double lo,
+                                         double hi, void* stream);
 
 /* Fills p with the benchmark defaults for a given coarsest resolution and level count. */
 void astg_default_params(astg_params* p, int coarsest, int levels);

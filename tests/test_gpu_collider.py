@@ -152,3 +152,23 @@ def test_sphere_collider_sdf_at_full_resolution():
     o.set("collider_sphere", [0.5, 0.5, 0.45, 0.1])
     assert_same("collider_sdf", o.get("collider_sdf"), s.get("collider_sdf"))
     s.close()
+
+
+def test_refine_split_map_on_the_device_equals_the_reference():
+    """astg_refine_split_map_device on CUDA tensors gives the reference's refined map (fixture made by
+    refineSplitMapByObstacleSdf itself), pass by pass, and refuses host memory."""
+    import torch
+
+    import ast_solver
+    from oracle.oracle import Oracle
+
+    g = golden("ref_refine_c16_l3")
+    c, lv, _ = g["meta/case"].tolist()
+    split = torch.tensor(np.ascontiguousarray(Oracle(c, lv).get("split_map"), dtype=np.int32).ravel(), device="cuda")
+    sdf = torch.tensor(np.ascontiguousarray(g["collider_sdf"], dtype=np.float64).ravel(), device="cuda")
+    for level, lo, hi in g["meta/refine"].tolist():
+        ast_solver.refine_split_map_tensor(split, int(level), sdf, (lo, hi))
+    torch.cuda.synchronize()
+    assert np.array_equal(split.cpu().numpy(), g["split_map"].ravel())
+    with pytest.raises(ValueError):
+        ast_solver.refine_split_map_tensor(split.cpu(), 1, sdf, (0.0, 1.0))
