@@ -917,6 +917,8 @@ struct astg_handle {
             ck(cudaEventCreate(&M.e0), "event");
             ck(cudaEventCreate(&M.e1), "event");
         }
+        // dalloc zeroes on the handle's stream: done before any lane stream touches the memory
+        ck(cudaStreamSynchronize(st), "lanes");
     }
     void freeLanes() {
         for (Lane& L : lanes) {
