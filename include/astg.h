@@ -5,7 +5,10 @@
  * (OctreeOmniGridSolver3 / OmniBoundarySolver3 / PCGSolver).  Host callers pass plain pointers
  * and sizes; all device memory belongs to the handle; every call returns an astg_status and no
  * C++ exception crosses the boundary.  One CUDA stream per handle; a handle is
- * thread-compatible, not thread-safe.  Arrays exchanged through astg_get / astg_set are in the
+ * thread-compatible, not thread-safe.  Different handles may be driven from different host threads
+ * at the same time: their work runs side by side on the device (a step keeps one 16-SM cluster
+ * busy for most of its time), and each handle's results are the same as when it runs alone.
+ * Arrays exchanged through astg_get / astg_set are in the
  * reference's storage order (level-major, then the reference's layout index: non-ghost cells in
  * raster z-y-x order followed by ghosts in discovery order), so they can be compared with the
  * reference's own grids element by element.
