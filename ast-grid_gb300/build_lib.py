@@ -63,5 +63,25 @@ def build(force=False, verbose=False):
     return LIB
 
 
+EXAMPLE_SRC = os.path.join(HERE, "examples", "octree_smoke.cpp")
+EXAMPLE = os.path.join(BUILD, "octree_smoke")
+
+
+def build_example(force=False):
+    """examples/octree_smoke.cpp, a C++ program using only include/astg.h, linked against the
+    library (found next to it at run time)."""
+    lib = build(force=force)
+    if force or _stale(EXAMPLE, [EXAMPLE_SRC, lib, os.path.join(ROOT, "include", "astg.h")]):
+        cxx = os.environ.get("CXX", "g++")
+        cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"), EXAMPLE_SRC, "-o",
+               EXAMPLE + ".tmp", "-L", BUILD, "-lastgrid_gpu", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("example build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        os.replace(EXAMPLE + ".tmp", EXAMPLE)
+    return EXAMPLE
+
+
 if __name__ == "__main__":
     print(build(force=True, verbose=True))
+    print(build_example())

@@ -110,3 +110,12 @@ def test_refine_split_map_matches_reference():
     assert (split != before).sum() > 100
     assert np.array_equal(split, g["split_map"].ravel())
     assert L.astg_refine_split_map(split.ctypes.data, res - 1, 1, sdf.ctypes.data, 0.0, 1.0) == 1
+
+
+def test_cpp_example_builds_against_the_header_alone():
+    """examples/octree_smoke.cpp (a host program using only include/astg.h) compiles and links
+    against the library; it runs in tests/test_gpu_example.py."""
+    import build_lib
+
+    exe = build_lib.build_example()
+    assert os.path.isfile(exe) and os.access(exe, os.X_OK)
