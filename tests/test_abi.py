@@ -119,3 +119,20 @@ def test_cpp_example_builds_against_the_header_alone():
 
     exe = build_lib.build_example()
     assert os.path.isfile(exe) and os.access(exe, os.X_OK)
+
+
+def test_new_entry_points_refuse_bad_arguments_without_a_device():
+    """Argument checks of the collider, batch-solve and device-refinement entry points run before any
+    device work: a null handle or null arrays give ASTG_BAD_ARG (no GPU needed)."""
+    import ctypes
+
+    import ast_solver
+
+    L = ast_solver.lib()
+    assert L.astg_set_collider_sphere(None, 0.5, 0.5, 0.45, 0.1) == ast_solver.ASTG_BAD_ARG
+    one = (ctypes.c_int * 2)(0, 1)
+    val = (ctypes.c_double * 1)(1.0)
+    st = (ast_solver.SolveStats * 1)()
+    assert L.astg_solve_batch(None, 1, one, one, val, 1, val, val, 1e-6, 10, ast_solver.FP64, st, None,
+                              None) == ast_solver.ASTG_BAD_ARG
+    assert L.astg_refine_split_map_device(None, 8, 1, None, 0.0, 1.0, None) == ast_solver.ASTG_BAD_ARG
